@@ -1,0 +1,498 @@
+"""
+Benchmark: the bandwidth-bound float32 suite on one (or N replica) GB300.
+
+Workload (seed 0, numpy default_rng, drawn in this order):
+  X   = standard_normal (8192, 32768) float32          (1 GiB, larger than L2)
+  row = uniform[0.5, 2) (1, 32768);  col = uniform[0.5, 2) (8192, 1)
+  idx = integers(0, 2^28, 2^26) uint32
+  Xoshiro128pp(size=2^20, seed=0)
+One step, in order (all through the vulkpy API):
+  X op row, X op col for op in + - * / ** max min          14 launches, 8 B/el
+  Z = |X| + 1e-3; sqrt(Z), invsqrt(Z), log(Z), Z.sqrt(inplace)  6 launches, 8 B/el
+  E = exp(X * 1e-4)                                          2 launches, 8 B/el
+  sum, maximum, minimum, mean of X and prod of E over
+    axis 0, axis 1, None                                    15 reductions, 4 B/el
+  X.gather(idx)                                              12 B/index
+  rng.random / normal / randint into 2^28-element buffers    4 B/out + 32 B/state
+  X op= row, X op= col for op in + - * /  (in place)         8 launches, 8 B/el
+metric = algorithmic bytes of the step / step time (GB/s).  Inputs stay in
+HBM for `value`; the `e2e` leg uploads X, row, col, idx from pinned host
+memory and reads the reduction results and the final X back every step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ROWS, COLS = 8192, 32768
+N_IDX = 1 << 26
+PRNG_STATES = 1 << 20
+METRIC = "ew HBM GB/s (bandwidth suite, fp32 8192x32768)"
+BIN_OPS = ["__add__", "__sub__", "__mul__", "__truediv__", "__pow__", "max", "min"]
+INPLACE_OPS = ["__iadd__", "__isub__", "__imul__", "__itruediv__"]
+
+
+def step_bytes(rows, cols, n_idx, states):
+    n = rows * cols
+    b = 0
+    b += 14 * (8 * n) + 7 * 4 * cols + 7 * 4 * rows      # broadcast binary
+    b += 6 * 8 * n                                       # abs, +1e-3, 3 unary, in-place sqrt
+    b += 2 * 8 * n                                       # E = exp(X * 1e-4)
+    b += 15 * 4 * n + 5 * 4 * (cols + rows + 1)          # reductions (+ outputs)
+    b += 12 * n_idx                                      # gather
+    b += 3 * (4 * n + 32 * states)                       # PRNG random / normal / randint
+    b += 8 * (8 * n) + 4 * 4 * cols + 4 * 4 * rows       # in-place broadcast
+    return b
+
+
+def bcast_bytes(rows, cols):
+    return 8 * rows * cols + 4 * max(rows, cols)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu_index: str):
+        self.rows = []
+        self.proc = None
+        self.gpu_index = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", self.gpu_index], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = sorted({self.REASONS[i] for r in self.rows for i in range(4) if "Active" == r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------- GPU suite
+class Timer:
+    def __init__(self, vk, gpu):
+        from vulkpy_gb300 import _lib
+        import ctypes
+        self.C, self.lib, self.h = ctypes, _lib.lib, gpu.handle
+
+    def mark(self):
+        j = self.C.c_void_p()
+        assert self.lib.vkc_timer_record(self.h, self.C.byref(j)) == 0
+        return j
+
+    def ms(self, a, b):
+        out = self.C.c_float()
+        assert self.lib.vkc_job_elapsed_ms(a, b, self.C.byref(out)) == 0
+        return out.value
+
+    def free(self, *js):
+        for j in js:
+            self.lib.vkc_job_destroy(j)
+
+
+def run_step(vk, X, row, col, idx, rng, U, Nrm, I, timer=None, spans=None, keep=None):
+    """One step of the suite.  With `timer`, each broadcast-binary launch is
+    bracketed by timing markers appended to `spans`."""
+    for other in (row, col):
+        for op in BIN_OPS:
+            if timer is not None:
+                a = timer.mark()
+            r = getattr(X, op)(other)
+            if timer is not None:
+                spans.append((a, timer.mark()))
+            del r
+    Z = X.abs()
+    Z += 1e-3
+    for name in ("sqrt", "invsqrt", "log"):
+        t = getattr(Z, name)()
+        del t
+    Z.sqrt(inplace=True)
+    E = X * 1e-4
+    E.exp(inplace=True)
+    outs = []
+    for axis in (0, 1, None):
+        outs.append(X.sum(axis=axis))
+        outs.append(X.maximum(axis=axis))
+        outs.append(X.minimum(axis=axis))
+        outs.append(X.mean(axis=axis))
+        outs.append(E.prod(axis=axis))
+    g = X.gather(idx)
+    rng.random(buffer=U)
+    rng.normal(buffer=Nrm)
+    rng.randint(buffer=I)
+    for other in (row, col):
+        for op in INPLACE_OPS:
+            getattr(X, op)(other)
+    if keep is not None:
+        keep.extend(outs)
+    return outs, g
+
+
+def make_inputs(rows, cols, n_idx):
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((rows, cols), dtype=np.float32)
+    row = rng.uniform(0.5, 2.0, (1, cols)).astype(np.float32)
+    col = rng.uniform(0.5, 2.0, (rows, 1)).astype(np.float32)
+    idx = rng.integers(0, rows * cols, n_idx, dtype=np.uint32)
+    return X, row, col, idx
+
+
+def gpu_arm(args, rank, world, dist):
+    import vulkpy_gb300 as vk
+    from vulkpy_gb300 import _lib
+    import ctypes
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    gpu = vk.GPU(local)
+    rows, cols, n_idx, states = args.rows, args.cols, args.n_idx, args.states
+    Xh, rowh, colh, idxh = make_inputs(rows, cols, n_idx)
+    X = vk.Array(gpu, data=Xh)
+    row, col = vk.Array(gpu, data=rowh), vk.Array(gpu, data=colh)
+    idx = vk.U32Array(gpu, data=idxh)
+    rng = vk.random.Xoshiro128pp(gpu, size=states, seed=0)
+    n = rows * cols
+    U, Nrm, I = vk.Array(gpu, shape=(n,)), vk.Array(gpu, shape=(n,)), vk.U32Array(gpu, shape=(n,))
+    timer = Timer(vk, gpu)
+    nbytes = step_bytes(rows, cols, n_idx, states)
+
+    for _ in range(args.warmup):
+        run_step(vk, X, row, col, idx, rng, U, Nrm, I)
+    gpu.wait()
+
+    clocks = ClockSampler(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
+    clocks.start()
+    time.sleep(0.3)
+    spans = []
+    lc0 = ctypes.c_uint64()
+    _lib.lib.vkc_launch_count(ctypes.byref(lc0))
+    if dist is not None:
+        dist.barrier()
+    gpu.wait()
+    t0 = timer.mark()
+    for _ in range(args.steps):
+        run_step(vk, X, row, col, idx, rng, U, Nrm, I, timer=timer, spans=spans)
+    t1 = timer.mark()
+    gpu.wait()
+    lc1 = ctypes.c_uint64()
+    _lib.lib.vkc_launch_count(ctypes.byref(lc1))
+    ms_total = timer.ms(t0, t1)
+    clk = clocks.stop()
+    bc_ms = [timer.ms(a, b) for a, b in spans]
+    timer.free(t0, t1, *[j for s in spans for j in s])
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms_total], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t[0])
+    ms_step = ms_total / args.steps
+    value = world * nbytes / (ms_step * 1e-3) / 1e9
+    launches = int(lc1.value - lc0.value)
+
+    # roofline of the dominant kernel: the broadcast-binary launches
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    else:
+        peak, peak_src = 6800.0, "fallback 6.8 TB/s"
+    avg_bc = float(np.mean(bc_ms))
+    achieved = bcast_bytes(rows, cols) / (avg_bc * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath)).get("broadcast_binary_bytes_per_launch")
+    roofline = {"kernel": "k_bcast_rows (X op row / X op col)", "bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "algorithmic_bytes": bcast_bytes(rows, cols), "avg_ms": round(avg_bc, 4),
+                "launches_timed": len(bc_ms)}
+
+    # per-op breakdown from one extra, separately timed step (not in `value`)
+    breakdown = profile_ops(vk, gpu, timer, X, row, col, idx, rng, U, Nrm, I)
+
+    e2e = e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, dist)
+
+    result = {
+        "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (numpy default_rng seed 0)",
+        "config": {"workload": f"bandwidth suite: X ({rows},{cols}) fp32 N(0,1), row (1,{cols}), col ({rows},1) "
+                               f"U[0.5,2); 49 ops/step (see bench.py docstring)",
+                   "rows": rows, "cols": cols, "gather_indices": n_idx, "prng_states": states,
+                   "bytes_per_step": nbytes, "l2": "inputs larger than L2 (1 GiB per array), no flush",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roofline, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "ops_gbs": breakdown,
+    }
+    return result
+
+
+def profile_ops(vk, gpu, timer, X, row, col, idx, rng, U, Nrm, I):
+    rows, cols = X.shape
+    n = rows * cols
+    fams = {}
+
+    def timed(name, nbytes, fn):
+        a = timer.mark()
+        r = fn()
+        b = timer.mark()
+        gpu.wait()
+        ms = timer.ms(a, b)
+        timer.free(a, b)
+        fams.setdefault(name, []).append(nbytes / (ms * 1e-3) / 1e9)
+        return r
+
+    gpu.wait()
+    timed("bcast_row", 8 * n, lambda: X + row)
+    timed("bcast_col", 8 * n, lambda: X * col)
+    Z = timed("unary_abs", 8 * n, lambda: X.abs())
+    timed("unary_log", 8 * n, lambda: Z.log())
+    timed("scalar_mul", 8 * n, lambda: X * 1e-4)
+    timed("sum_axis0", 4 * n, lambda: X.sum(axis=0))
+    timed("sum_axis1", 4 * n, lambda: X.sum(axis=1))
+    timed("sum_all", 4 * n, lambda: X.sum())
+    timed("max_all", 4 * n, lambda: X.maximum())
+    timed("gather_12B", 12 * idx.size, lambda: X.gather(idx))
+    timed("prng_f32", 4 * n + 32 * rng.size, lambda: rng.random(buffer=U))
+    timed("prng_normal", 4 * n + 32 * rng.size, lambda: rng.normal(buffer=Nrm))
+    timed("prng_u32", 4 * n + 32 * rng.size, lambda: rng.randint(buffer=I))
+    timed("inplace_bcast", 8 * n, lambda: X.__iadd__(row))
+    X -= row
+    return {k: round(float(np.median(v)), 1) for k, v in fams.items()}
+
+
+def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, dist):
+    """Same step through the public API from pinned host buffers: uploads of
+    X, row, col, idx and read-back of the reductions and the final X are
+    inside the timed region."""
+    Xp = vk.vkarray.empty_pinned(Xh.shape)
+    Xp[...] = Xh
+    idxp = vk.vkarray.empty_pinned(idxh.shape, np.uint32)
+    idxp[...] = idxh
+    h2d = Xp.nbytes + rowh.nbytes + colh.nbytes + idxp.nbytes
+    d2h = 0
+
+    def one():
+        nonlocal d2h
+        X = vk.Array(gpu, data=Xp)
+        row, col = vk.Array(gpu, data=rowh), vk.Array(gpu, data=colh)
+        idx = vk.U32Array(gpu, data=idxp)
+        outs, g = run_step(vk, X, row, col, idx, rng, U, Nrm, I)
+        got = [np.asarray(o) for o in outs]
+        final = np.asarray(X)
+        d2h = sum(o.nbytes for o in got) + final.nbytes
+        return final
+
+    for _ in range(max(1, args.warmup)):
+        one()
+    gpu.wait()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        one()
+    gpu.wait()
+    dt = (time.perf_counter() - t0) / args.e2e_steps
+    if dist is not None:
+        import torch
+        t = torch.tensor([dt], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t[0])
+    return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+            "api": "vulkpy_gb300 public API (Array(data=pinned), ops, np.asarray)"}
+
+
+# ---------------------------------------------------------------- CPU oracle
+def cpu_suite_pass(O, X, row, col, idx, st, sizes):
+    """The same step on the CPU restatement (oracle/vkoracle.c), OpenMP."""
+    L = O.lib()
+    p = lambda a: a.ctypes.data
+    rows, cols = X.shape
+    n = X.size
+    out = np.empty_like(X)
+    sa = np.array([rows, cols], np.int64)
+    for other in (row, col):
+        so = np.array(other.shape, np.int64)
+        for op in range(7):
+            L.bcast_binary(op, p(X), p(sa), p(other), p(so), p(out), p(sa), 2)
+    Z = np.empty_like(X)
+    L.ew_unary(0, p(X), p(Z), n)
+    L.ew_scalar(0, p(Z), np.float32(1e-3), p(Z), n)
+    for op in (18, 19, 15):
+        L.ew_unary(op, p(Z), p(out), n)
+    L.ew_unary(18, p(Z), p(Z), n)
+    E = np.empty_like(X)
+    L.ew_scalar(2, p(X), np.float32(1e-4), p(E), n)
+    L.ew_unary(14, p(E), p(E), n)
+    r0 = np.empty(cols, np.float32)
+    r1 = np.empty(rows, np.float32)
+    for src, ops in ((X, (0, 2, 3, 0)), (E, (1,))):
+        for op in ops:
+            L.reduce_axis(op, p(src), 1, rows, cols, p(r0))
+            L.reduce_axis(op, p(src), rows, cols, 1, p(r1))
+            L.reduce_all(op, p(src), n)
+    g = np.empty(idx.size, np.float32)
+    L.gather(p(X), n, p(idx), idx.size, p(g))
+    states, m = sizes
+    L.xo_generate(p(st), states, p(out), n, 1)
+    L.xo_generate(p(st), states, p(out), n, 1)
+    L.box_muller(p(out), p(out), n, np.float32(0), np.float32(1))
+    L.xo_generate(p(st), states, p(out), n, 0)
+    for other in (row, col):
+        so = np.array(other.shape, np.int64)
+        for op in range(4):
+            L.bcast_binary(op, p(X), p(sa), p(other), p(so), p(X), p(sa), 2)
+
+
+def cpu_sample(args):
+    """A bounded sample of the workload: the first `rows` rows, indices and
+    PRNG states scaled by the same factor."""
+    rows = args.cpu_rows
+    frac = rows / args.rows
+    X, row, col, idx = make_inputs(args.rows, args.cols, args.n_idx)
+    Xs = np.ascontiguousarray(X[:rows])
+    cols_ = np.ascontiguousarray(col[:rows])
+    n_idx = int(args.n_idx * frac)
+    idxs = np.ascontiguousarray(idx[:n_idx] % np.uint32(Xs.size))
+    states = max(1, int(args.states * frac))
+    del X
+    return Xs, row, cols_, idxs, states, n_idx
+
+
+_CPU_CACHE = {}
+
+
+def _cpu_data(args):
+    from oracle import ops as O  # checker / CPU baseline only
+    if "data" not in _CPU_CACHE:
+        Xs, row, col, idx, states, n_idx = cpu_sample(args)
+        _CPU_CACHE["data"] = (Xs, row, col, idx, O.Xoshiro128pp(0, states).state, states, n_idx)
+    return _CPU_CACHE["data"]
+
+
+def cpu_measure_once(args) -> float:
+    from oracle import ops as O
+    Xs, row, col, idx, st, states, n_idx = _cpu_data(args)
+    t0 = time.perf_counter()
+    cpu_suite_pass(O, Xs, row, col, idx, st, (states, 0))
+    return time.perf_counter() - t0
+
+
+def cpu_info(args):
+    import oracle
+    Xs, row, col, idx, st, states, n_idx = _cpu_data(args)
+    return step_bytes(Xs.shape[0], Xs.shape[1], n_idx, states), oracle.lib().oracle_threads(), Xs.shape
+
+
+def cpu_baseline(args):
+    nbytes, threads, shape = cpu_info(args)
+    cpu_measure_once(args)  # warm-up
+    times = [cpu_measure_once(args) for _ in range(args.cpu_passes)]
+    best = min(times)
+    return {"value": round(nbytes / best / 1e9, 2), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"{shape[0]} of {args.rows} rows ({shape[0] * shape[1] * 4 / 2**20:.0f} MiB), indices and "
+                      f"PRNG states scaled alike; best of {len(times)} passes of the step on the CPU restatement "
+                      f"of the reference's shaders (oracle/vkoracle.c, OpenMP)"}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    nbytes, threads, shape = cpu_info(args)
+    for _ in range(args.warmup):
+        cpu_measure_once(args)
+    times = [cpu_measure_once(args) for _ in range(args.steps)]
+    dt = float(np.mean(times))
+    value = nbytes / dt / 1e9
+    sample = (f"{shape[0]} of {args.rows} rows per step, indices and PRNG states scaled alike; "
+              f"CPU restatement of the reference's shaders (oracle/vkoracle.c), OpenMP over all host threads")
+    return {"metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (numpy default_rng seed 0)",
+            "impl": "reference",
+            "config": {"workload": f"bandwidth suite, bounded sample on host cores ({shape[0]}x{shape[1]})",
+                       "bytes_per_step": nbytes},
+            "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rows", type=int, default=ROWS)
+    ap.add_argument("--cols", type=int, default=COLS)
+    ap.add_argument("--n-idx", type=int, default=N_IDX)
+    ap.add_argument("--states", type=int, default=PRNG_STATES)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-rows", type=int, default=256)
+    ap.add_argument("--cpu-passes", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        tdist.init_process_group("gloo")
+        dist = tdist
+
+    if args.impl == "reference":
+        res = reference_arm(args, rank, world)
+        if res is not None:
+            print(json.dumps(res), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    res = gpu_arm(args, rank, world, dist)
+    if rank == 0:
+        if not args.no_cpu:
+            res["cpu_baseline"] = cpu_baseline(args)
+        print(json.dumps(res), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+/*
+ * vulkpy_gb300.h -- C ABI of the GB300 (sm_103a) array engine.
+ *
+ * This is the drop-in boundary that replaces vulkpy's native module
+ * `_vkarray` (vulkpy/_vkarray.cc:756-898, pybind11) and the GLSL compute
+ * shaders it dispatches (vulkpy/shader/*.comp).  Every entry point takes
+ * plain pointers and sizes, returns an int status (VKC_OK == 0), and
+ * records a message retrievable with vkc_last_error() on failure.
+ *
+ * Memory passed to the compute entry points is device memory obtained from
+ * vkc_alloc() (or any device pointer valid in the device's CUDA context).
+ * All work is issued, in order, on the device's compute stream; nothing
+ * blocks the host except the explicit wait / copy-to-host calls.
+ *
+ * Each declaration names the reference interface it replaces (file:line,
+ * paths inside the vulkpy project).
+ */
+#ifndef VULKPY_GB300_H
+#define VULKPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define VKC_OK            0
+#define VKC_ERR_INVALID   1  /* bad argument (shape, size, op code, NULL)   */
+#define VKC_ERR_OOM       2  /* device or pinned host allocation failed      */
+#define VKC_ERR_CUDA      3  /* a CUDA runtime / driver call failed           */
+#define VKC_ERR_TIMEOUT   4  /* vkc_job_wait deadline passed (not an error of the GPU) */
+
+/* ---- op codes -------------------------------------------------------- */
+/* binary / scalar ops: vulkpy/shader/{add,sub,mul,div,pow,max,min}*.comp,
+ * r{sub,div,pow}_scalar.comp */
+enum vkc_binary_op {
+  VKC_ADD = 0, VKC_SUB = 1, VKC_MUL = 2, VKC_DIV = 3,
+  VKC_POW = 4, VKC_MAX = 5, VKC_MIN = 6,
+  VKC_RSUB = 7, VKC_RDIV = 8, VKC_RPOW = 9  /* reversed: op(other, self) */
+};
+
+/* unary ops: vulkpy/shader/{abs,sign,sin,...,invsqrt}.comp */
+enum vkc_unary_op {
+  VKC_ABS = 0, VKC_SIGN = 1, VKC_SIN = 2, VKC_COS = 3, VKC_TAN = 4,
+  VKC_ASIN = 5, VKC_ACOS = 6, VKC_ATAN = 7, VKC_SINH = 8, VKC_COSH = 9,
+  VKC_TANH = 10, VKC_ASINH = 11, VKC_ACOSH = 12, VKC_ATANH = 13,
+  VKC_EXP = 14, VKC_LOG = 15, VKC_EXP2 = 16, VKC_LOG2 = 17,
+  VKC_SQRT = 18, VKC_INVSQRT = 19,
+  VKC_COPY = 20          /* identity; used by broadcast_to */
+};
+
+/* reductions: vulkpy/shader/{sum,prod,maximum,minimum}{,_v1.3,_axis,_axis_rebroadcast}.comp */
+enum vkc_reduce_op { VKC_SUM = 0, VKC_PROD = 1, VKC_MAXIMUM = 2, VKC_MINIMUM = 3 };
+
+/* summation precision for VKC_SUM / VKC_PROD over axis=None */
+enum vkc_reduce_precision {
+  VKC_RED_PLAIN = 0,        /* per-thread sequential fp32, tree combine          */
+  VKC_RED_PAIRWISE = 1,     /* 16 fp32 accumulators per thread, tree combine      */
+  VKC_RED_COMPENSATED = 2   /* Neumaier per thread, TwoSum tree, fp64 cross-block */
+};
+
+/* matmul arithmetic */
+enum vkc_matmul_precision {
+  VKC_MM_FP32 = 0,   /* SIMT fp32 FMA (the drop-in default)                   */
+  VKC_MM_BF16 = 1,   /* tcgen05 bf16 x bf16 -> fp32 accumulate                */
+  VKC_MM_BF16X3 = 2  /* tcgen05 split-bf16: hi*hi + hi*lo + lo*hi, fp32 acc   */
+};
+
+/* activation fused into the Dense epilogue */
+enum vkc_activation { VKC_ACT_NONE = 0, VKC_ACT_RELU = 1, VKC_ACT_SIGMOID = 2 };
+
+typedef struct vkc_device* vkc_device_t;  /* one GPU + its streams        */
+typedef struct vkc_job* vkc_job_t;        /* completion marker (an event) */
+
+/* ---- errors ---------------------------------------------------------- */
+/* Message of the last failing call on this thread ("" if none).
+ * Replaces the std::runtime_error texts of vulkpy/_vkarray.cc:32,286,451,454,508. */
+const char* vkc_last_error(void);
+/* Library version string. */
+const char* vkc_version(void);
+
+/* ---- device: vulkpy/_vkarray.cc:460-574 (class GPU), createGPU 759-763 ---- */
+int vkc_device_count(int* count);
+/* Open GPU `index`.  `priority` in [0,1] maps to a CUDA stream priority
+ * (replaces the queue priority of _vkarray.cc:472-485). */
+int vkc_device_open(int index, float priority, vkc_device_t* out);
+int vkc_device_close(vkc_device_t dev);
+/* Block until all work issued on the device is done (GPU.wait, _vkarray.cc:560-562). */
+int vkc_device_synchronize(vkc_device_t dev);
+/* The cudaStream_t all compute entry points use (as void*). */
+int vkc_device_stream(vkc_device_t dev, void** stream);
+/* Route subsequent work to `stream` (a cudaStream_t of the same device, e.g.
+ * torch's current stream); NULL restores the device's own stream. */
+int vkc_device_set_stream(vkc_device_t dev, void* stream);
+/* Number of SMs and the device name (for logs and grid sizing). */
+int vkc_device_info(vkc_device_t dev, int* sm_count, char* name, size_t name_len);
+/* Read-and-clear the device error word: bit0 = a gather index was out of
+ * range.  Synchronises the compute stream. */
+int vkc_device_check_errors(vkc_device_t dev, uint32_t* flags);
+
+/* ---- memory: Buffer<T> (_vkarray.cc:38-130), GPU::toBuffer/createBuffer ---- */
+/* Stream-ordered device allocation on the compute stream (cudaMallocAsync).
+ * Size 0 returns NULL and VKC_OK. */
+int vkc_alloc(vkc_device_t dev, size_t bytes, void** ptr);
+/* Stream-ordered free: safe while kernels that use `ptr` are still queued. */
+int vkc_free(vkc_device_t dev, void* ptr);
+/* Pinned (page-locked) host memory, for host mirrors and fast copies. */
+int vkc_host_alloc(size_t bytes, void** ptr);
+int vkc_host_free(void* ptr);
+/* Upload into NEW device memory on the copy stream: allocates `bytes`,
+ * copies from `src`, makes the compute stream wait for the copy, and blocks
+ * the host only until the copy itself is done (not queued compute work).
+ * Replaces GPU::toBuffer (_vkarray.cc:511-517, Buffer ctor 81-86). */
+int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void** dptr);
+/* Host->device copy into existing memory, ordered after queued compute work.
+ * A pageable `src` is staged before the call returns.  A pinned `src` is
+ * read when the stream reaches the copy: keep it unchanged until `*job`
+ * completes (pass job = NULL only for pageable sources). */
+int vkc_h2d(vkc_device_t dev, void* dst, const void* src, size_t bytes, vkc_job_t* job);
+/* Device->host copy after all queued compute work; blocks until done.
+ * Replaces the mapped-memory read of _GPUArray.__array__ (vkarray.py:186-188). */
+int vkc_d2h(vkc_device_t dev, void* dst, const void* src, size_t bytes);
+/* Fill n floats with v (zeros(), Constant initializer; vkarray.py:1524-1542). */
+int vkc_fill_f32(vkc_device_t dev, float* dst, size_t n, float v);
+int vkc_fill_u32(vkc_device_t dev, uint32_t* dst, size_t n, uint32_t v);
+int vkc_copy(vkc_device_t dev, void* dst, const void* src, size_t bytes);
+
+/* ---- jobs: class Job (_vkarray.cc:392-457), Job.wait(timeout) 876-879 ---- */
+/* Marker for "everything issued so far"; wait() on it = Array.wait(). */
+int vkc_job_record(vkc_device_t dev, vkc_job_t* job);
+/* Wait with a deadline (timeout_ns < 0: no deadline).  Returns VKC_ERR_TIMEOUT
+ * with "Timeout at Command Wait" like _vkarray.cc:451. */
+int vkc_job_wait(vkc_job_t job, int64_t timeout_ns);
+/* *done = 1 when complete, 0 otherwise (non-blocking). */
+int vkc_job_query(vkc_job_t job, int* done);
+int vkc_job_destroy(vkc_job_t job);
+/* Timing marker (a CUDA event with timing) on the compute stream, and the
+ * elapsed milliseconds between two completed markers.  No reference
+ * counterpart (vulkpy has no timers); used for CUDA-event benchmarking. */
+int vkc_timer_record(vkc_device_t dev, vkc_job_t* job);
+int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms);
+/* Number of kernels this library has launched since load (all devices). */
+int vkc_launch_count(uint64_t* count);
+
+/* ---- elementwise ---------------------------------- */
+/* c[i] = a[i] op b[i] for i < n; c may alias a or b (in-place i*.comp twins).
+ * vulkpy/vkarray.py:440-452 (_opVec/_opVec3), shaders add.comp:20-26 etc. */
+int vkc_binary(vkc_device_t dev, int op, const float* a, const float* b, float* c, size_t n);
+/* c[i] = a[i] op s  (op < VKC_RSUB), or s op' a[i] for VKC_RSUB/RDIV/RPOW.
+ * vkarray.py:469-483 (_opVecScalar*), add_scalar.comp:19-24, rsub_scalar.comp. */
+int vkc_binary_scalar(vkc_device_t dev, int op, const float* a, float s, float* c, size_t n);
+/* c[i] = f(a[i]); c may alias a.  vkarray.py:680-1098, exp.comp:18-23 etc. */
+int vkc_unary(vkc_device_t dev, int op, const float* a, float* c, size_t n);
+/* d[i] = min(max(a[i], lo), hi) with lo/hi arrays (lo_arr/hi_arr non-NULL,
+ * length n) or scalars.  vkarray.py:1110-1191, clamp{,_sv,_vs,_ss}.comp. */
+int vkc_clamp(vkc_device_t dev, const float* a, const float* lo_arr, const float* hi_arr,
+              float lo, float hi, float* d, size_t n);
+
+/* ---- broadcasting --------------------------------- */
+/* numpy broadcasting of a and b into c.  Shapes are given right-aligned and
+ * already padded to `ndim` (<= 16) entries; a dim of 1 broadcasts.  c may
+ * alias a when a has c's shape (in-place i*_broadcast.comp).
+ * vkarray.py:499-519, 538-557; add_broadcast.comp:25-45, iadd_broadcast.comp:22-41. */
+int vkc_broadcast_binary(vkc_device_t dev, int op,
+                         const float* a, const int64_t* a_shape,
+                         const float* b, const int64_t* b_shape,
+                         float* c, const int64_t* c_shape, int ndim);
+/* c = clamp(a, lo, hi) with every operand broadcast to c_shape; lo/hi NULL
+ * means the scalar lo_s/hi_s.  Replaces clamp's broadcast_to copies (vkarray.py:1147-1160). */
+int vkc_broadcast_clamp(vkc_device_t dev,
+                        const float* a, const int64_t* a_shape,
+                        const float* lo, const int64_t* lo_shape, float lo_s,
+                        const float* hi, const int64_t* hi_shape, float hi_s,
+                        float* c, const int64_t* c_shape, int ndim);
+/* Explicit broadcast copy.  vkarray.py:1434-1474, broadcast.comp:25-44. */
+int vkc_broadcast_to(vkc_device_t dev, const float* a, const int64_t* a_shape,
+                     float* c, const int64_t* c_shape, int ndim);
+
+/* ---- reductions -------------------------------------------- */
+/* out[0] = reduce(a[0..n)) * scale (scale applies to SUM/PROD only; pass 1).
+ * vkarray.py:1246-1274 (axis=None), sum.comp:18-30, sum_v1.3.comp:20-29. */
+int vkc_reduce_all(vkc_device_t dev, int op, int precision, const float* a, size_t n,
+                   float* out, float scale);
+/* View a as [prev, axis, post]; out[i, j] = reduce_k a[i, k, j] * scale.
+ * With rebroadcast != 0, out has a's shape and every k gets the result.
+ * vkarray.py:1194-1244, sum_axis.comp:20-32, sum_axis_rebroadcast.comp:20-35. */
+int vkc_reduce_axis(vkc_device_t dev, int op, const float* a, size_t prev, size_t axis,
+                    size_t post, float* out, int rebroadcast, float scale);
+
+/* ---- matmul ----------------------------------------------------- */
+/* C[M,N] = A[M,K] @ B[K,N], row-major fp32 in and out.
+ * vkarray.py:585-605, matmul.comp:23-33. */
+int vkc_matmul(vkc_device_t dev, int precision, const float* a, const float* b, float* c,
+               int64_t m, int64_t k, int64_t n);
+/* General form used by the nn layers: C = alpha * op(A) @ op(B) + beta * C,
+ * op(X) = X or X^T (trans flags), leading dimensions in elements. */
+int vkc_gemm(vkc_device_t dev, int precision, int trans_a, int trans_b,
+             int64_t m, int64_t n, int64_t k, float alpha,
+             const float* a, int64_t lda, const float* b, int64_t ldb,
+             float beta, float* c, int64_t ldc);
+
+/* ---- gather ------------------------------------------------------ */
+/* c[i] = a[idx[i]], i < n_idx.  An index >= n_a writes NaN and sets bit0 of
+ * the device error word.  vkarray.py:1476-1500, gather.comp:21-26. */
+int vkc_gather(vkc_device_t dev, const float* a, size_t n_a, const uint32_t* idx,
+               size_t n_idx, float* c);
+/* c[k, i, j] = a[i, min(idx[k], axis-1), j]; output [n_idx, prev, post].
+ * vkarray.py:1501-1521, gather_axis.comp:24-43, U32Array.to_onehot 239-253. */
+int vkc_gather_axis(vkc_device_t dev, const float* a, size_t prev, size_t axis, size_t post,
+                    const uint32_t* idx, size_t n_idx, float* c);
+
+/* ---- xoshiro128++ PRNG ---------------------------------------- */
+/* Fill state[4*size] (device) exactly like PRNG::Xoshiro128pp's constructor
+ * (_vkarray.cc:643-675): four chained splitmix64 words, then state i is the
+ * reference's jump() applied i times, computed in parallel on the GPU from
+ * precomputed powers of the (linear, GF(2)) jump map. */
+int vkc_xoshiro_seed(vkc_device_t dev, uint64_t seed, uint32_t size, uint32_t* state);
+/* n outputs from `size` states with the reference's chunked layout:
+ * out[k] = next^(k / size)(state[k % size]); states advance in place.
+ * Replaces Xoshiro128pp::random (_vkarray.cc:697-717) and
+ * prng_xoshiro128pp_{uint32,float}.comp:26-44.  One launch per call. */
+int vkc_xoshiro_u32(vkc_device_t dev, uint32_t* state, uint32_t size, uint32_t* out, size_t n);
+int vkc_xoshiro_f32(vkc_device_t dev, uint32_t* state, uint32_t size, float* out, size_t n);
+/* Normal numbers: the uniform stream of vkc_xoshiro_f32 of length n (n even)
+ * or n+1 (n odd) transformed pairwise by Box-Muller, fused in one launch when
+ * `size` is even.  random.py:60-124, prng_{i,}box_muller.comp. */
+int vkc_xoshiro_normal(vkc_device_t dev, uint32_t* state, uint32_t size, float* out, size_t n,
+                       float mean, float stddev);
+/* Box-Muller on an existing uniform buffer u[0..2*ceil(n/2)) into out[0..n)
+ * (out may alias u).  prng_box_muller.comp:19-32, prng_ibox_muller.comp:16-27. */
+int vkc_box_muller(vkc_device_t dev, const float* u, float* out, size_t n, float mean, float stddev);
+/* out[i] = low + uint(float(high_incl - low + 1) * u_i) with u_i drawn from
+ * the state stream (fused).  random.py:126-186, prng_randrange.comp:20-27. */
+int vkc_xoshiro_randrange(vkc_device_t dev, uint32_t* state, uint32_t size, uint32_t* out,
+                          size_t n, uint32_t low, uint32_t high_incl);
+
+/* ---- nn fused kernels ---------------------------------------- */
+/* y[b,o] = act(sum_i w[o,i] x[b,i] + bias[o]).  nn/layers.py:94-102, batch_affine.comp:25-39. */
+int vkc_dense_forward(vkc_device_t dev, int precision, const float* x, const float* w,
+                      const float* bias, float* y, int64_t batch, int64_t in_dim,
+                      int64_t out_dim, int act);
+/* Given dy (already multiplied by the activation derivative when act != NONE
+ * is applied by the caller), accumulate dW += dy^T x, db += sum_b dy and write
+ * dx = dy @ w (dx may be NULL).  nn/layers.py:104-141 without the (B,out,in)
+ * temporary of layers.py:131-135. */
+int vkc_dense_backward(vkc_device_t dev, int precision, const float* x, const float* w,
+                       const float* dy, float* dx, float* dw, float* db,
+                       int64_t batch, int64_t in_dim, int64_t out_dim);
+/* Row softmax over the last axis of [rows, cols] (nn/layers.py:297-300). */
+int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols);
+/* loss_rows[r] = sum_c -y log(p + 1e-8) with p = softmax(x) when softmax != 0
+ * (else p = x); nn_cross_entropy.comp:21-26, losses.py:140-176, 218-249. */
+int vkc_cross_entropy(vkc_device_t dev, const float* x, const float* y, float* loss_rows,
+                      float* p_out, int64_t rows, int64_t cols, int softmax);
+/* Adam step (optimizers.py:221-253) on n parameters, fused:
+ * m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
+ * value += -lr * (m / (1-b1t)) / (sqrt(v / (1-b2t)) + eps).  beta1t/beta2t
+ * are the running powers after this step's update.  Hyper-parameters are
+ * doubles (Python floats): each scalar is formed in double and rounded to
+ * float32 exactly where the reference hands it to a float32 array op, so
+ * the result is bit-identical to the reference's unfused chain. */
+int vkc_adam_update(vkc_device_t dev, float* value, const float* grad, float* m, float* v,
+                    size_t n, double lr, double beta1, double beta2, double eps,
+                    double beta1t, double beta2t);
+/* value += (-lr) * grad (optimizers.py:39-52). */
+int vkc_sgd_update(vkc_device_t dev, float* value, const float* grad, size_t n, double lr);
+/* h += g^2; value += (g / (sqrt(h) + eps)) * (-lr)  (optimizers.py:120-139). */
+int vkc_adagrad_update(vkc_device_t dev, float* value, const float* grad, float* h, size_t n,
+                       double lr, double eps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VULKPY_GB300_H */

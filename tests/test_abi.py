@@ -1,0 +1,47 @@
+"""The C-ABI library loads and exports every symbol include/vulkpy_gb300.h declares
+(no compute calls: runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "vulkpy_gb300.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(vkc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert len(syms) >= 45
+    assert "vkc_binary" in syms and "vkc_xoshiro_seed" in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from vulkpy_gb300 import _lib
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_binding_covers_header():
+    from vulkpy_gb300 import _lib
+    assert set(declared_symbols()) <= set(_lib.exported_symbols())
+
+
+def test_version_and_error_strings():
+    from vulkpy_gb300 import _lib
+    assert b"sm_103a" in _lib.lib.vkc_version()
+    assert isinstance(_lib.last_error(), str)
+
+
+def test_null_device_is_rejected_without_gpu():
+    from vulkpy_gb300 import _lib
+    st = _lib.lib.vkc_binary(None, _lib.ADD, None, None, None, 4)
+    assert st == _lib.ERR_INVALID
+    assert "NULL" in _lib.last_error()

@@ -1,0 +1,105 @@
+"""nn kernels on the GPU against float32 / float64 restatements of the
+reference's layer, loss and optimizer math (vulkpy/nn/*.py).
+
+Optimizers are bit-exact: the fused kernels reproduce the reference's chain
+of float32 array ops (optimizers.py:39-52, 120-139, 221-253), restated here
+op by op in numpy float32 (no fused multiply-add)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+f32 = np.float32
+
+
+@pytest.fixture(scope="module")
+def vk():
+    import vulkpy_gb300
+    return vulkpy_gb300
+
+
+def adam_reference(value, grad, m, v, b1t, b2t, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+    m = (m * f32(beta1)).astype(f32)
+    m = (m + (f32(1 - beta1) * grad).astype(f32)).astype(f32)
+    v = (v * f32(beta2)).astype(f32)
+    v = (v + (f32(1 - beta2) * (grad * grad).astype(f32)).astype(f32)).astype(f32)
+    b1t *= beta1
+    b2t *= beta2
+    mhat = (m / f32(1 - b1t)).astype(f32)
+    vhat = (v / f32(1 - b2t)).astype(f32)
+    vhat = np.sqrt(vhat).astype(f32)
+    vhat = (vhat + f32(eps)).astype(f32)
+    mhat = (mhat * f32(-lr)).astype(f32)
+    mhat = (mhat / vhat).astype(f32)
+    return (value + mhat).astype(f32), m, v, b1t, b2t
+
+
+def test_adam_bit_exact_over_steps(gpu, vk):
+    rng = np.random.default_rng(0)
+    n = 100003
+    value = rng.standard_normal(n).astype(f32)
+    p = vk.nn.Parameter(gpu, (n,), opt=vk.nn.Adam(gpu, lr=1e-3), initializer=lambda g, s: vk.Array(g, data=value))
+    m = np.zeros(n, f32); v = np.zeros(n, f32); b1t = b2t = 1.0
+    val = value.copy()
+    for step in range(4):
+        grad = rng.standard_normal(n).astype(f32) * f32(10 ** (step - 2))
+        p.grad[:] = 0.0
+        p.add_grad(vk.Array(gpu, data=grad))
+        p.update()
+        val, m, v, b1t, b2t = adam_reference(val, grad, m, v, b1t, b2t)
+        np.testing.assert_array_equal(np.asarray(p.value), val)
+        np.testing.assert_array_equal(np.asarray(p.opt_state.m), m)
+        np.testing.assert_array_equal(np.asarray(p.opt_state.v), v)
+
+
+def test_sgd_and_adagrad_bit_exact(gpu, vk):
+    rng = np.random.default_rng(1)
+    n = 4099
+    g = rng.standard_normal(n).astype(f32)
+    v0 = rng.standard_normal(n).astype(f32)
+    p = vk.nn.Parameter(gpu, (n,), opt=vk.nn.SGD(0.01), initializer=lambda gg, s: vk.Array(gg, data=v0))
+    p.add_grad(vk.Array(gpu, data=g))
+    p.update()
+    np.testing.assert_array_equal(np.asarray(p.value), (v0 + (f32(-0.01) * g).astype(f32)).astype(f32))
+    q = vk.nn.Parameter(gpu, (n,), opt=vk.nn.AdaGrad(gpu, lr=0.05, tau=0.1), initializer=lambda gg, s: vk.Array(gg, data=v0))
+    q.add_grad(vk.Array(gpu, data=g))
+    q.update()
+    h = (np.full(n, f32(0.1)) + (g * g).astype(f32)).astype(f32)
+    r = (g / (np.sqrt(h).astype(f32) + f32(1e-8)).astype(f32)).astype(f32)
+    r = (r * f32(-0.05)).astype(f32)
+    np.testing.assert_array_equal(np.asarray(q.value), (v0 + r).astype(f32))
+
+
+@pytest.mark.parametrize("B,I,Out", [(1, 1, 1), (2, 3, 4), (33, 65, 17), (256, 784, 1024), (7, 1024, 10)])
+def test_dense_forward_backward(gpu, vk, B, I, Out):
+    rng = np.random.default_rng(B * I + Out)
+    x = rng.standard_normal((B, I)).astype(f32)
+    W = rng.standard_normal((Out, I)).astype(f32) * f32(0.1)
+    b = rng.standard_normal(Out).astype(f32)
+    dy = rng.standard_normal((B, Out)).astype(f32)
+    d = vk.nn.Dense(gpu, I, Out, w_init=lambda g, s: vk.Array(g, data=W), b_init=lambda g, s: vk.Array(g, data=b))
+    X = vk.Array(gpu, data=x)
+    y = np.asarray(d(X))
+    x64, W64 = x.astype(np.float64), W.astype(np.float64)
+    y64 = x64 @ W64.T + b
+    np.testing.assert_allclose(y, y64, rtol=1e-5, atol=1e-5 * np.sqrt(I))
+    dx = np.asarray(d.backward(vk.Array(gpu, data=dy)))
+    np.testing.assert_allclose(dx, dy.astype(np.float64) @ W64, rtol=1e-5, atol=1e-5 * np.sqrt(Out))
+    np.testing.assert_allclose(np.asarray(d.w.grad), dy.astype(np.float64).T @ x64, rtol=1e-5,
+                               atol=1e-5 * np.sqrt(B))
+    np.testing.assert_allclose(np.asarray(d.b.grad), dy.astype(np.float64).sum(0), rtol=1e-5, atol=1e-5 * np.sqrt(B))
+
+
+def test_softmax_cross_entropy_rows(gpu, vk):
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((300, 10)).astype(f32) * 3
+    y = np.eye(10, dtype=f32)[rng.integers(0, 10, 300)]
+    sce = vk.nn.SoftmaxCrossEntropyLoss()
+    L = np.asarray(sce(vk.Array(gpu, data=x), vk.Array(gpu, data=y)))
+    x64 = x.astype(np.float64)
+    p = np.exp(x64 - x64.max(1, keepdims=True))
+    p /= p.sum(1, keepdims=True)
+    Lr = (-y * np.log(p + 1e-8)).sum(1).mean()
+    np.testing.assert_allclose(L, [Lr], rtol=1e-5)
+    np.testing.assert_allclose(np.asarray(sce.grad()), (p - y) / 300, rtol=1e-5, atol=1e-7)
+    sm = vk.nn.Softmax()
+    np.testing.assert_allclose(np.asarray(sm(vk.Array(gpu, data=x))), p, rtol=1e-5, atol=1e-7)

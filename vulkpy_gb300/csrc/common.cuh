@@ -1,0 +1,85 @@
+// Internal definitions shared by the runtime and the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <cstdio>
+#include <cstdarg>
+#include <atomic>
+#include <mutex>
+#include <string>
+
+#include "../../include/vulkpy_gb300.h"
+
+#define VKC_EXPORT extern "C" __attribute__((visibility("default")))
+
+struct vkc_device {
+  int index = 0;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  cudaStream_t own_stream = nullptr;   // compute stream created at open
+  cudaStream_t stream = nullptr;       // current compute stream (own or user's)
+  cudaStream_t copy_stream = nullptr;  // uploads into fresh buffers
+  cudaEvent_t copy_done = nullptr;     // reused marker for uploads
+  uint32_t* err_word = nullptr;        // device error flags (bit0: gather index)
+  uint32_t* xo_jump_pows = nullptr;    // xoshiro jump-map powers (lazy)
+  uint32_t* xo_next_pows = nullptr;    // xoshiro next-map powers (lazy)
+  std::mutex mu;
+  char name[256] = {0};
+};
+
+struct vkc_job {
+  cudaEvent_t ev = nullptr;
+  int device = 0;
+};
+
+namespace vkc {
+
+// Record an error message for vkc_last_error() and return `code`.
+int set_error(int code, const char* fmt, ...);
+void clear_error();
+
+// Make `dev` current on this thread; returns VKC_OK or an error code.
+int bind(vkc_device_t dev);
+
+extern std::atomic<uint64_t> g_launches;  // kernels launched (all devices)
+
+inline int check_launch(const char* what) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "%s launch: %s", what, cudaGetErrorString(e));
+  return VKC_OK;
+}
+
+// Grid for a grid-stride streaming kernel with `threads` per block.
+inline unsigned stream_grid(const vkc_device* dev, size_t work_items, int threads, int blocks_per_sm = 8) {
+  size_t want = (work_items + threads - 1) / threads;
+  size_t cap = (size_t)dev->sm_count * blocks_per_sm;
+  if (want < 1) want = 1;
+  return (unsigned)(want < cap ? want : cap);
+}
+
+// Stream-ordered scratch allocation on the device's current stream.
+int scratch_alloc(vkc_device_t dev, size_t bytes, void** p);
+void scratch_free(vkc_device_t dev, void* p);
+
+}  // namespace vkc
+
+#define VKC_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e__ = (call);                                                            \
+    if (e__ != cudaSuccess)                                                              \
+      return vkc::set_error(VKC_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e__));     \
+  } while (0)
+
+#define VKC_REQUIRE(cond, ...)                                                           \
+  do {                                                                                   \
+    if (!(cond)) return vkc::set_error(VKC_ERR_INVALID, __VA_ARGS__);                    \
+  } while (0)
+
+#define VKC_BIND(dev)                                                                    \
+  do {                                                                                   \
+    int r__ = vkc::bind(dev);                                                            \
+    if (r__ != VKC_OK) return r__;                                                       \
+  } while (0)

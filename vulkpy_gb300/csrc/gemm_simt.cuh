@@ -1,0 +1,136 @@
+// FP32 SIMT GEMM: C = act(alpha * op(A) op(B) + beta * C + bias[n]).
+//
+// The plain-precision path of matmul.comp:23-33 (one invocation per output
+// with a serial K loop and uncoalesced B reads).  128x128 block tile, K
+// steps of 8, 256 threads each owning an 8x8 register tile split 4+4 in both
+// directions so shared-memory reads are conflict-free float4s; the next
+// K-step is prefetched into registers while the current one is multiplied
+// out of a double-buffered shared tile.  Within one output the K terms are
+// accumulated in order (k = 0, 1, 2, ...) with FMA.
+#pragma once
+#include "common.cuh"
+
+namespace vkc {
+
+constexpr int kGemmBM = 128, kGemmBN = 128, kGemmBK = 8, kGemmThreads = 256;
+
+struct GemmEpilogue {
+  const float* bias = nullptr;  // per output column, may be NULL
+  int act = VKC_ACT_NONE;
+};
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(kGemmThreads)
+k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restrict__ A, int64_t lda,
+            const float* __restrict__ B, int64_t ldb, float beta, float* C, int64_t ldc, GemmEpilogue epi) {
+  __shared__ __align__(16) float As[2][kGemmBK][kGemmBM];
+  __shared__ __align__(16) float Bs[2][kGemmBK][kGemmBN];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int64_t m0 = (int64_t)blockIdx.y * kGemmBM;
+  const int64_t n0 = (int64_t)blockIdx.x * kGemmBN;
+
+  // Each thread loads 4 elements of the A tile and 4 of the B tile per K step.
+  // op(A)(m,k) = TA ? A[k*lda + m] : A[m*lda + k]; op(B)(k,n) = TB ? B[n*ldb + k] : B[k*ldb + n].
+  float ra[4], rb[4];
+  auto load_a = [&](int64_t k0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int e = tid + i * kGemmThreads;  // 0..1023 over (m: 128, k: 8)
+      int mm, kk;
+      if (TA) { mm = e & 127; kk = e >> 7; }   // contiguous along m
+      else { kk = e & 7; mm = e >> 3; }        // contiguous along k
+      int64_t gm = m0 + mm, gk = k0 + kk;
+      ra[i] = (gm < M && gk < K) ? (TA ? A[gk * lda + gm] : A[gm * lda + gk]) : 0.f;
+    }
+  };
+  auto load_b = [&](int64_t k0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int e = tid + i * kGemmThreads;
+      int nn, kk;
+      if (TB) { kk = e & 7; nn = e >> 3; }     // contiguous along k
+      else { nn = e & 127; kk = e >> 7; }      // contiguous along n
+      int64_t gn = n0 + nn, gk = k0 + kk;
+      rb[i] = (gn < N && gk < K) ? (TB ? B[gn * ldb + gk] : B[gk * ldb + gn]) : 0.f;
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int e = tid + i * kGemmThreads;
+      if (TA) As[buf][e >> 7][e & 127] = ra[i];
+      else As[buf][e & 7][e >> 3] = ra[i];
+      if (TB) Bs[buf][e & 7][e >> 3] = rb[i];
+      else Bs[buf][e >> 7][e & 127] = rb[i];
+    }
+  };
+
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+  const int64_t ksteps = (K + kGemmBK - 1) / kGemmBK;
+  load_a(0);
+  load_b(0);
+  store(0);
+  __syncthreads();
+  for (int64_t ks = 0; ks < ksteps; ++ks) {
+    const int buf = ks & 1;
+    if (ks + 1 < ksteps) {
+      load_a((ks + 1) * kGemmBK);
+      load_b((ks + 1) * kGemmBK);
+    }
+#pragma unroll
+    for (int kk = 0; kk < kGemmBK; ++kk) {
+      float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+      float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4 + 64]);
+      float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+      float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4 + 64]);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    if (ks + 1 < ksteps) {
+      store(buf ^ 1);
+      __syncthreads();
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int64_t gm = m0 + ty * 4 + (i & 3) + (i >> 2) * 64;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      int64_t gn = n0 + tx * 4 + (j & 3) + (j >> 2) * 64;
+      if (gn >= N) continue;
+      float v = alpha * acc[i][j];
+      if (beta != 0.f) v += beta * C[gm * ldc + gn];
+      if (epi.bias) v += epi.bias[gn];
+      if (epi.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+      else if (epi.act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+      C[gm * ldc + gn] = v;
+    }
+  }
+}
+
+inline int gemm_simt(vkc_device_t dev, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
+                     const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                     GemmEpilogue epi) {
+  if (M == 0 || N == 0) return VKC_OK;
+  dim3 grid((unsigned)((N + kGemmBN - 1) / kGemmBN), (unsigned)((M + kGemmBM - 1) / kGemmBM));
+  VKC_REQUIRE(grid.y <= 65535, "matmul: M too large for the SIMT grid");
+  if (!ta && !tb) k_gemm_simt<false, false><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  else if (ta && !tb) k_gemm_simt<true, false><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  else if (!ta && tb) k_gemm_simt<false, true><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  else k_gemm_simt<true, true><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  return check_launch("gemm_simt");
+}
+
+}  // namespace vkc

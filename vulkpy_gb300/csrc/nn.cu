@@ -1,0 +1,234 @@
+// Fused kernels for the nn layers, losses and optimizers.
+//
+//   Dense forward  (nn/layers.py:94-102, batch_affine.comp:25-39): a GEMM
+//     x W^T with bias (and optional activation) applied in the epilogue.
+//   Dense backward (nn/layers.py:104-141): dW += dy^T x and dx = dy W as two
+//     GEMMs; the reference materialises dy[:,:,None]*x[:,None,:] (B*out*in
+//     floats, 1 GiB at 256x1024x1024) and sums it over the batch.
+//   Softmax / cross entropy (layers.py:297-300, losses.py:113-149,
+//     nn_cross_entropy.comp:21-26): one warp per row.
+//   Optimizers (optimizers.py:39-52, 120-139, 221-253): one pass over the
+//     parameters, reproducing the reference's sequence of float32 array ops
+//     (each intermediate rounded, no FMA contraction), so the update is
+//     bit-identical to the unfused chain.
+#include "common.cuh"
+#include "gemm_simt.cuh"
+#include "gemm_tc.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
+             const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+             vkc::GemmEpilogue epi) {
+  if (precision == VKC_MM_FP32)
+    return vkc::gemm_simt(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  if (precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3)
+    return vkc::gemm_tc(dev, precision, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  return vkc::set_error(VKC_ERR_INVALID, "unknown matmul precision %d", precision);
+}
+
+// db[o] += sum_b dy[b, o]
+__global__ void k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
+  int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= out_dim) return;
+  float s = 0.f;
+  for (int64_t b = 0; b < batch; ++b) s += dy[b * out_dim + o];
+  db[o] += s;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// y = exp(x - max) / sum(exp(x - max)) per row, as layers.py:297-300 orders it.
+__global__ void __launch_bounds__(kThreads)
+k_softmax(const float* x, float* y, int64_t rows, int64_t cols) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= rows) return;
+  const float* xr = x + r * cols;
+  float* yr = y + r * cols;
+  float m = -INFINITY;
+  for (int64_t c = lane; c < cols; c += 32) m = fmaxf(m, xr[c]);
+  m = warp_max(m);
+  float s = 0.f;
+  for (int64_t c = lane; c < cols; c += 32) s += expf(xr[c] - m);
+  s = warp_sum(s);
+  for (int64_t c = lane; c < cols; c += 32) yr[c] = expf(xr[c] - m) / s;
+}
+
+// loss_rows[r] = sum_c -y * log(p + 1e-8), p = softmax(x) or x.
+__global__ void __launch_bounds__(kThreads)
+k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, int64_t rows, int64_t cols,
+                int softmax) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= rows) return;
+  const float* xr = x + r * cols;
+  const float* yr = y + r * cols;
+  float m = 0.f, s = 1.f;
+  if (softmax) {
+    m = -INFINITY;
+    for (int64_t c = lane; c < cols; c += 32) m = fmaxf(m, xr[c]);
+    m = warp_max(m);
+    s = 0.f;
+    for (int64_t c = lane; c < cols; c += 32) s += expf(xr[c] - m);
+    s = warp_sum(s);
+  }
+  float L = 0.f;
+  for (int64_t c = lane; c < cols; c += 32) {
+    float p = softmax ? expf(xr[c] - m) / s : xr[c];
+    if (p_out) p_out[r * cols + c] = p;
+    L += (-yr[c]) * logf(p + 1e-8f);
+  }
+  L = warp_sum(L);
+  if (lane == 0) loss_rows[r] = L;
+}
+
+// The reference's Adam chain (optimizers.py:235-253), one element per step:
+//   m *= b1; m += c1*g; v *= b2; v += c2*g^2;
+//   mhat = m/d1; vhat = sqrt(v/d2) + eps; mhat *= -lr; mhat /= vhat; value += mhat
+__global__ void __launch_bounds__(kThreads)
+k_adam(float* value, const float* grad, float* m, float* v, size_t n, float b1, float c1, float b2, float c2,
+       float d1, float d2, float eps, float nlr) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float g = grad[i];
+    float mi = __fadd_rn(__fmul_rn(m[i], b1), __fmul_rn(c1, g));
+    float vi = __fadd_rn(__fmul_rn(v[i], b2), __fmul_rn(c2, __fmul_rn(g, g)));
+    m[i] = mi;
+    v[i] = vi;
+    float mhat = __fdiv_rn(mi, d1);
+    float vhat = __fadd_rn(__fsqrt_rn(__fdiv_rn(vi, d2)), eps);
+    mhat = __fmul_rn(mhat, nlr);
+    mhat = __fdiv_rn(mhat, vhat);
+    value[i] = __fadd_rn(value[i], mhat);
+  }
+}
+
+// SGD (optimizers.py:39-52): diff = (-lr) * g; value += diff.
+__global__ void __launch_bounds__(kThreads) k_sgd(float* value, const float* grad, size_t n, float nlr) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    value[i] = __fadd_rn(value[i], __fmul_rn(nlr, grad[i]));
+}
+
+// AdaGrad (optimizers.py:120-139): h += g^2; r = g / (sqrt(h) + eps); r *= -lr; value += r.
+__global__ void __launch_bounds__(kThreads)
+k_adagrad(float* value, const float* grad, float* h, size_t n, float nlr, float eps) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float g = grad[i];
+    float hi = __fadd_rn(h[i], __fmul_rn(g, g));
+    h[i] = hi;
+    float r = __fdiv_rn(g, __fadd_rn(__fsqrt_rn(hi), eps));
+    r = __fmul_rn(r, nlr);
+    value[i] = __fadd_rn(value[i], r);
+  }
+}
+
+}  // namespace
+
+VKC_EXPORT int vkc_dense_forward(vkc_device_t dev, int precision, const float* x, const float* w, const float* bias,
+                                 float* y, int64_t batch, int64_t in_dim, int64_t out_dim, int act) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
+  if (batch == 0 || out_dim == 0) return VKC_OK;
+  VKC_REQUIRE(x && w && y, "NULL buffer");
+  VKC_REQUIRE(act >= VKC_ACT_NONE && act <= VKC_ACT_SIGMOID, "unknown activation %d", act);
+  vkc::GemmEpilogue epi;
+  epi.bias = bias;
+  epi.act = act;
+  // y[B,out] = x[B,in] @ W[out,in]^T
+  return gemm_any(dev, precision, false, true, batch, out_dim, in_dim, 1.0f, x, in_dim, w, in_dim, 0.0f, y, out_dim,
+                  epi);
+}
+
+VKC_EXPORT int vkc_dense_backward(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy,
+                                  float* dx, float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
+  if (batch == 0) return VKC_OK;
+  VKC_REQUIRE(x && w && dy, "NULL buffer");
+  int r = VKC_OK;
+  if (db) {
+    unsigned grid = (unsigned)((out_dim + kThreads - 1) / kThreads);
+    k_colsum_acc<<<grid, kThreads, 0, dev->stream>>>(dy, batch, out_dim, db);
+    r = vkc::check_launch("dense_backward db");
+    if (r != VKC_OK) return r;
+  }
+  if (dw) {
+    // dW[out,in] += dy[B,out]^T @ x[B,in]
+    r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw, in_dim,
+                 vkc::GemmEpilogue{});
+    if (r != VKC_OK) return r;
+  }
+  if (dx) {
+    // dx[B,in] = dy[B,out] @ W[out,in]
+    r = gemm_any(dev, precision, false, false, batch, in_dim, out_dim, 1.0f, dy, out_dim, w, in_dim, 0.0f, dx, in_dim,
+                 vkc::GemmEpilogue{});
+  }
+  return r;
+}
+
+VKC_EXPORT int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols) {
+  VKC_BIND(dev);
+  if (rows <= 0 || cols <= 0) return VKC_OK;
+  VKC_REQUIRE(x && y, "NULL buffer");
+  unsigned grid = (unsigned)((rows * 32 + kThreads - 1) / kThreads);
+  k_softmax<<<grid, kThreads, 0, dev->stream>>>(x, y, rows, cols);
+  return vkc::check_launch("softmax");
+}
+
+VKC_EXPORT int vkc_cross_entropy(vkc_device_t dev, const float* x, const float* y, float* loss_rows, float* p_out,
+                                 int64_t rows, int64_t cols, int softmax) {
+  VKC_BIND(dev);
+  if (rows <= 0) return VKC_OK;
+  VKC_REQUIRE(x && y && loss_rows, "NULL buffer");
+  unsigned grid = (unsigned)((rows * 32 + kThreads - 1) / kThreads);
+  k_cross_entropy<<<grid, kThreads, 0, dev->stream>>>(x, y, loss_rows, p_out, rows, cols, softmax);
+  return vkc::check_launch("cross_entropy");
+}
+
+VKC_EXPORT int vkc_adam_update(vkc_device_t dev, float* value, const float* grad, float* m, float* v, size_t n,
+                               double lr, double beta1, double beta2, double eps, double beta1t, double beta2t) {
+  VKC_BIND(dev);
+  if (n == 0) return VKC_OK;
+  VKC_REQUIRE(value && grad && m && v, "NULL buffer");
+  // Scalars as the reference forms them: Python doubles rounded to float32
+  // at the array op that consumes them (optimizers.py:235-251).
+  const float b1 = (float)beta1, b2 = (float)beta2;
+  const float c1 = (float)(1.0 - beta1), c2 = (float)(1.0 - beta2);
+  const float d1 = (float)(1.0 - beta1t), d2 = (float)(1.0 - beta2t);
+  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  k_adam<<<grid, kThreads, 0, dev->stream>>>(value, grad, m, v, n, b1, c1, b2, c2, d1, d2, (float)eps, (float)(-lr));
+  return vkc::check_launch("adam");
+}
+
+VKC_EXPORT int vkc_sgd_update(vkc_device_t dev, float* value, const float* grad, size_t n, double lr) {
+  VKC_BIND(dev);
+  if (n == 0) return VKC_OK;
+  VKC_REQUIRE(value && grad, "NULL buffer");
+  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  k_sgd<<<grid, kThreads, 0, dev->stream>>>(value, grad, n, (float)(-lr));
+  return vkc::check_launch("sgd");
+}
+
+VKC_EXPORT int vkc_adagrad_update(vkc_device_t dev, float* value, const float* grad, float* h, size_t n, double lr,
+                                  double eps) {
+  VKC_BIND(dev);
+  if (n == 0) return VKC_OK;
+  VKC_REQUIRE(value && grad && h, "NULL buffer");
+  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  k_adagrad<<<grid, kThreads, 0, dev->stream>>>(value, grad, h, n, (float)(-lr), (float)eps);
+  return vkc::check_launch("adagrad");
+}

@@ -1,0 +1,349 @@
+// Device, stream, memory and job management: the CUDA replacement for the
+// Vulkan runtime of vulkpy/_vkarray.cc (class GPU 460-574, Buffer<T> 38-130,
+// Job 392-457).  One compute stream per opened device; all kernels and
+// copies that touch existing buffers are ordered on it, so dependent ops need
+// no host waits (the reference waits on fences, _vkarray.cc:430-432).
+#include "common.cuh"
+
+#include <chrono>
+#include <thread>
+#include <cstring>
+
+namespace vkc {
+
+std::atomic<uint64_t> g_launches{0};
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int bind(vkc_device_t dev) {
+  if (!dev) return set_error(VKC_ERR_INVALID, "device handle is NULL");
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (cur != dev->index) {
+    e = cudaSetDevice(dev->index);
+    if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  }
+  return VKC_OK;
+}
+
+int scratch_alloc(vkc_device_t dev, size_t bytes, void** p) {
+  *p = nullptr;
+  if (bytes == 0) return VKC_OK;
+  cudaError_t e = cudaMallocAsync(p, bytes, dev->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  return VKC_OK;
+}
+
+void scratch_free(vkc_device_t dev, void* p) {
+  if (p) cudaFreeAsync(p, dev->stream);
+}
+
+}  // namespace vkc
+
+using namespace vkc;
+
+VKC_EXPORT const char* vkc_last_error(void) { return g_last_error.c_str(); }
+
+VKC_EXPORT const char* vkc_version(void) { return "vulkpy_gb300 0.1.0 (sm_103a)"; }
+
+VKC_EXPORT int vkc_device_count(int* count) {
+  VKC_REQUIRE(count, "count is NULL");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *count = 0;
+    return set_error(VKC_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+  }
+  *count = n;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_open(int index, float priority, vkc_device_t* out) {
+  VKC_REQUIRE(out, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  int r = vkc_device_count(&n);
+  if (r != VKC_OK) return r;
+  VKC_REQUIRE(index >= 0 && index < n, "GPU index %d out of range (%d devices)", index, n);
+  VKC_CUDA(cudaSetDevice(index));
+
+  auto* dev = new vkc_device();
+  dev->index = index;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, index);
+  if (e != cudaSuccess) {
+    delete dev;
+    return set_error(VKC_ERR_CUDA, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+  }
+  dev->sm_count = prop.multiProcessorCount;
+  dev->cc_major = prop.major;
+  dev->cc_minor = prop.minor;
+  std::snprintf(dev->name, sizeof(dev->name), "%s", prop.name);
+
+  // Map priority in [0,1] onto the device's stream priority range
+  // (greatest priority is the numerically lowest value).
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  float p = priority < 0.f ? 0.f : (priority > 1.f ? 1.f : priority);
+  int prio = lo + (int)((hi - lo) * p);
+  e = cudaStreamCreateWithPriority(&dev->own_stream, cudaStreamNonBlocking, prio);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->copy_stream, cudaStreamNonBlocking, prio);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->copy_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&dev->err_word, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(dev->err_word, 0, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    delete dev;
+    return set_error(VKC_ERR_CUDA, "device setup: %s", cudaGetErrorString(e));
+  }
+  dev->stream = dev->own_stream;
+
+  // Keep freed blocks cached in the pool instead of returning them to the OS:
+  // arrays are short-lived and large (up to GiBs), re-mapping is expensive.
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, index) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  cudaGetLastError();
+  *out = dev;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
+  if (!dev) return VKC_OK;
+  VKC_BIND(dev);
+  cudaStreamSynchronize(dev->own_stream);
+  if (dev->stream != dev->own_stream) cudaStreamSynchronize(dev->stream);
+  cudaStreamSynchronize(dev->copy_stream);
+  if (dev->err_word) cudaFree(dev->err_word);
+  if (dev->xo_jump_pows) cudaFree(dev->xo_jump_pows);
+  if (dev->xo_next_pows) cudaFree(dev->xo_next_pows);
+  cudaEventDestroy(dev->copy_done);
+  cudaStreamDestroy(dev->own_stream);
+  cudaStreamDestroy(dev->copy_stream);
+  delete dev;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_synchronize(vkc_device_t dev) {
+  VKC_BIND(dev);
+  VKC_CUDA(cudaStreamSynchronize(dev->copy_stream));
+  VKC_CUDA(cudaStreamSynchronize(dev->stream));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_stream(vkc_device_t dev, void** stream) {
+  VKC_REQUIRE(dev && stream, "NULL argument");
+  *stream = (void*)dev->stream;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_set_stream(vkc_device_t dev, void* stream) {
+  VKC_REQUIRE(dev, "device handle is NULL");
+  dev->stream = stream ? (cudaStream_t)stream : dev->own_stream;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_info(vkc_device_t dev, int* sm_count, char* name, size_t name_len) {
+  VKC_REQUIRE(dev, "device handle is NULL");
+  if (sm_count) *sm_count = dev->sm_count;
+  if (name && name_len) std::snprintf(name, name_len, "%s", dev->name);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_device_check_errors(vkc_device_t dev, uint32_t* flags) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(flags, "flags is NULL");
+  uint32_t h = 0;
+  VKC_CUDA(cudaMemcpyAsync(&h, dev->err_word, sizeof(h), cudaMemcpyDeviceToHost, dev->stream));
+  VKC_CUDA(cudaMemsetAsync(dev->err_word, 0, sizeof(uint32_t), dev->stream));
+  VKC_CUDA(cudaStreamSynchronize(dev->stream));
+  *flags = h;
+  return VKC_OK;
+}
+
+// ---- memory ---------------------------------------------------------------
+
+VKC_EXPORT int vkc_alloc(vkc_device_t dev, size_t bytes, void** ptr) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(ptr, "ptr is NULL");
+  return scratch_alloc(dev, bytes, ptr);
+}
+
+VKC_EXPORT int vkc_free(vkc_device_t dev, void* ptr) {
+  if (!ptr) return VKC_OK;
+  VKC_BIND(dev);
+  VKC_CUDA(cudaFreeAsync(ptr, dev->stream));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_host_alloc(size_t bytes, void** ptr) {
+  VKC_REQUIRE(ptr, "ptr is NULL");
+  *ptr = nullptr;
+  if (bytes == 0) return VKC_OK;
+  cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return set_error(VKC_ERR_OOM, "cudaHostAlloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_host_free(void* ptr) {
+  if (!ptr) return VKC_OK;
+  VKC_CUDA(cudaFreeHost(ptr));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void** dptr) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(dptr && (src || bytes == 0), "NULL argument");
+  *dptr = nullptr;
+  if (bytes == 0) return VKC_OK;
+  std::lock_guard<std::mutex> lk(dev->mu);
+  // Allocate and copy on the copy stream so that the upload does not queue
+  // behind compute work; the compute stream then waits for the copy.
+  cudaError_t e = cudaMallocAsync(dptr, bytes, dev->copy_stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *dptr = nullptr;
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  VKC_CUDA(cudaMemcpyAsync(*dptr, src, bytes, cudaMemcpyHostToDevice, dev->copy_stream));
+  VKC_CUDA(cudaEventRecord(dev->copy_done, dev->copy_stream));
+  VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->copy_done, 0));
+  VKC_CUDA(cudaEventSynchronize(dev->copy_done));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_h2d(vkc_device_t dev, void* dst, const void* src, size_t bytes, vkc_job_t* job) {
+  VKC_BIND(dev);
+  if (job) *job = nullptr;
+  if (bytes == 0) return VKC_OK;
+  VKC_REQUIRE(dst && src, "NULL argument");
+  // A pageable source is staged before cudaMemcpyAsync returns; a pinned
+  // one is read when the stream reaches the copy, which `job` marks.
+  VKC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, dev->stream));
+  if (job) return vkc_job_record(dev, job);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_d2h(vkc_device_t dev, void* dst, const void* src, size_t bytes) {
+  VKC_BIND(dev);
+  if (bytes == 0) return VKC_OK;
+  VKC_REQUIRE(dst && src, "NULL argument");
+  VKC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, dev->stream));
+  VKC_CUDA(cudaStreamSynchronize(dev->stream));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_copy(vkc_device_t dev, void* dst, const void* src, size_t bytes) {
+  VKC_BIND(dev);
+  if (bytes == 0) return VKC_OK;
+  VKC_REQUIRE(dst && src, "NULL argument");
+  VKC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, dev->stream));
+  return VKC_OK;
+}
+
+// ---- jobs -------------------------------------------------------------------
+
+VKC_EXPORT int vkc_job_record(vkc_device_t dev, vkc_job_t* job) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(job, "job is NULL");
+  auto* j = new vkc_job();
+  j->device = dev->index;
+  cudaError_t e = cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(j->ev, dev->stream);
+  if (e != cudaSuccess) {
+    if (j->ev) cudaEventDestroy(j->ev);
+    delete j;
+    *job = nullptr;
+    return set_error(VKC_ERR_CUDA, "job record: %s", cudaGetErrorString(e));
+  }
+  *job = j;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_job_wait(vkc_job_t job, int64_t timeout_ns) {
+  if (!job) return VKC_OK;
+  if (timeout_ns < 0) {
+    cudaError_t e = cudaEventSynchronize(job->ev);
+    if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "Error at Command Wait: %s", cudaGetErrorString(e));
+    return VKC_OK;
+  }
+  // Poll against a host deadline; the GPU keeps running, nothing is aborted.
+  auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(timeout_ns);
+  for (;;) {
+    cudaError_t e = cudaEventQuery(job->ev);
+    if (e == cudaSuccess) return VKC_OK;
+    if (e != cudaErrorNotReady) return set_error(VKC_ERR_CUDA, "Error at Command Wait: %s", cudaGetErrorString(e));
+    if (std::chrono::steady_clock::now() >= deadline) {
+      cudaGetLastError();
+      return set_error(VKC_ERR_TIMEOUT, "Timeout at Command Wait");
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+VKC_EXPORT int vkc_job_query(vkc_job_t job, int* done) {
+  VKC_REQUIRE(done, "done is NULL");
+  if (!job) { *done = 1; return VKC_OK; }
+  cudaError_t e = cudaEventQuery(job->ev);
+  if (e == cudaSuccess) { *done = 1; return VKC_OK; }
+  if (e == cudaErrorNotReady) { cudaGetLastError(); *done = 0; return VKC_OK; }
+  return set_error(VKC_ERR_CUDA, "Error at Command Wait: %s", cudaGetErrorString(e));
+}
+
+VKC_EXPORT int vkc_timer_record(vkc_device_t dev, vkc_job_t* job) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(job, "job is NULL");
+  auto* j = new vkc_job();
+  j->device = dev->index;
+  cudaError_t e = cudaEventCreate(&j->ev);
+  if (e == cudaSuccess) e = cudaEventRecord(j->ev, dev->stream);
+  if (e != cudaSuccess) {
+    if (j->ev) cudaEventDestroy(j->ev);
+    delete j;
+    *job = nullptr;
+    return set_error(VKC_ERR_CUDA, "timer record: %s", cudaGetErrorString(e));
+  }
+  *job = j;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms) {
+  VKC_REQUIRE(start && end && ms, "NULL argument");
+  VKC_CUDA(cudaEventSynchronize(end->ev));
+  VKC_CUDA(cudaEventElapsedTime(ms, start->ev, end->ev));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_launch_count(uint64_t* count) {
+  VKC_REQUIRE(count, "count is NULL");
+  *count = vkc::g_launches.load(std::memory_order_relaxed);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_job_destroy(vkc_job_t job) {
+  if (!job) return VKC_OK;
+  cudaEventDestroy(job->ev);
+  delete job;
+  return VKC_OK;
+}
