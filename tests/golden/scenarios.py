@@ -242,7 +242,7 @@ def prng_streams(vk):
     return out
 
 
-@scenario(tol=("ulp", 8))
+@scenario(tol=("rtol", 1e-6, 4e-6))
 def prng_normal_even(vk):
     g = vk.GPU()
     out = {}
@@ -254,7 +254,7 @@ def prng_normal_even(vk):
     return out
 
 
-@scenario(tol=("ulp", 8))
+@scenario(tol=("rtol", 1e-6, 4e-6))
 def prng_normal_odd(vk):
     # Odd n draws n+1 uniforms.  The reference dispatches n//2 pairs, but
     # whole 64-wide workgroups run, so the last element is written unless
@@ -445,7 +445,7 @@ def small_suite_prng(vk):
             "after": A(r.randint(shape=(256,)))}
 
 
-@scenario(tol=("ulp", 16))
+@scenario(tol=("rtol", 1e-6, 4e-6))
 def small_suite_normal(vk):
     g = vk.GPU()
     r = vk.random.Xoshiro128pp(g, size=64, seed=0)

@@ -16,7 +16,7 @@ LIB_PATH = Path(os.environ.get("VULKPY_GB300_LIB", _HERE / "libvulkpy_gb300.so")
 if not LIB_PATH.exists():
     raise ImportError(
         f"vulkpy_gb300 native library not found at {LIB_PATH}; "
-        "build it with `python -m vulkpy_gb300.build` (needs nvcc)")
+        "build it with `python vulkpy_gb300/build.py` (needs nvcc)")
 
 lib = C.CDLL(str(LIB_PATH))
 

@@ -11,8 +11,10 @@
 //     post > 1 -> threads own 4 consecutive columns (coalesced) and walk the
 //     axis; when prev*post is too small to fill 152 SMs the axis is split
 //     into slices whose partials a second kernel combines.
-// Summation is compensated (Neumaier per thread, TwoSum when merging) by
-// default; plain and pairwise modes exist for the precision study.
+// Sums are compensated by default (Neumaier per thread, TwoSum when
+// merging) and so are products (FMA-based error term: float32 products of
+// values near 1 otherwise drift by ~0.1 ulp per factor); plain and pairwise
+// modes exist for the precision study.
 #include "common.cuh"
 
 #include <algorithm>
@@ -57,6 +59,13 @@ struct Acc {
       float t = s + x;
       c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
       s = t;
+    } else if constexpr (OP == VKC_PROD && COMP) {
+      // Compensated product (Graillat): the exact rounding error of s*x is
+      // fma(s, x, -p); c carries the accumulated error of the product.
+      float p = s * x;
+      float e = fmaf(s, x, -p);
+      c = fmaf(c, x, e);
+      s = p;
     } else {
       s = combine<OP>(s, x);
     }
@@ -69,11 +78,17 @@ struct Acc {
       float err = (s - (t - bp)) + (os - bp);
       s = t;
       c = c + oc + err;
+    } else if constexpr (OP == VKC_PROD && COMP) {
+      // (s + c)(os + oc) ~ s*os + [err(s*os) + s*oc + c*os]
+      float p = s * os;
+      float e = fmaf(s, os, -p);
+      c = fmaf(s, oc, fmaf(c, os, e));
+      s = p;
     } else {
       s = combine<OP>(s, os);
     }
   }
-  __device__ __forceinline__ float value() const { return (OP == VKC_SUM && COMP) ? s + c : s; }
+  __device__ __forceinline__ float value() const { return COMP ? s + c : s; }
 };
 
 template <int OP, bool COMP>
@@ -479,8 +494,9 @@ VKC_EXPORT int vkc_reduce_all(vkc_device_t dev, int op, int precision, const flo
       if (precision == VKC_RED_PAIRWISE) return reduce_all_impl<VKC_SUM, false, 16>(dev, a, n, out, scale);
       return reduce_all_impl<VKC_SUM, false, 1>(dev, a, n, out, scale);
     case VKC_PROD:
-      if (precision == VKC_RED_PLAIN) return reduce_all_impl<VKC_PROD, false, 1>(dev, a, n, out, scale);
-      return reduce_all_impl<VKC_PROD, false, 16>(dev, a, n, out, scale);
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_impl<VKC_PROD, true, 1>(dev, a, n, out, scale);
+      if (precision == VKC_RED_PAIRWISE) return reduce_all_impl<VKC_PROD, false, 16>(dev, a, n, out, scale);
+      return reduce_all_impl<VKC_PROD, false, 1>(dev, a, n, out, scale);
     case VKC_MAXIMUM: return reduce_all_impl<VKC_MAXIMUM, false, 1>(dev, a, n, out, scale);
     case VKC_MINIMUM: return reduce_all_impl<VKC_MINIMUM, false, 1>(dev, a, n, out, scale);
     default: return vkc::set_error(VKC_ERR_INVALID, "unknown reduce op %d", op);
@@ -495,7 +511,7 @@ VKC_EXPORT int vkc_reduce_axis(vkc_device_t dev, int op, const float* a, size_t 
   if (prev == 0 || post == 0) return VKC_OK;
   switch (op) {
     case VKC_SUM: return reduce_axis_impl<VKC_SUM, true>(dev, a, prev, axis, post, out, rebroadcast, scale);
-    case VKC_PROD: return reduce_axis_impl<VKC_PROD, false>(dev, a, prev, axis, post, out, rebroadcast, scale);
+    case VKC_PROD: return reduce_axis_impl<VKC_PROD, true>(dev, a, prev, axis, post, out, rebroadcast, scale);
     case VKC_MAXIMUM: return reduce_axis_impl<VKC_MAXIMUM, false>(dev, a, prev, axis, post, out, rebroadcast, scale);
     case VKC_MINIMUM: return reduce_axis_impl<VKC_MINIMUM, false>(dev, a, prev, axis, post, out, rebroadcast, scale);
     default: return vkc::set_error(VKC_ERR_INVALID, "unknown reduce op %d", op);
