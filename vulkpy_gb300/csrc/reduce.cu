@@ -79,11 +79,15 @@ struct Acc {
       s = t;
       c = c + oc + err;
     } else if constexpr (OP == VKC_PROD && COMP) {
-      // (s + c)(os + oc) ~ s*os + [err(s*os) + s*oc + c*os]
+      // (s + c)(os + oc) ~ s*os + [err(s*os) + s*oc + c*os], then
+      // renormalise (Fast2Sum) so |c| stays below an ulp of s and the
+      // dropped c*oc term is negligible in long merge trees.
       float p = s * os;
       float e = fmaf(s, os, -p);
-      c = fmaf(s, oc, fmaf(c, os, e));
-      s = p;
+      float cc = fmaf(s, oc, fmaf(c, os, e));
+      float t = p + cc;
+      c = cc - (t - p);
+      s = t;
     } else {
       s = combine<OP>(s, os);
     }
