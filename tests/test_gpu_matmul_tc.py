@@ -1,0 +1,80 @@
+"""Tensor-core (tcgen05) matmul: bf16 and split-bf16x3 against float64.
+
+Bounds (relative Frobenius error vs float64, N(0,1) inputs):
+  * bf16:    operands rounded to 8 significant bits -> ~3e-3; bound 8e-3.
+  * bf16x3:  hi/lo split keeps ~16 bits per operand -> a few 1e-6; bound 1e-5
+             (the accuracy target for the split method).
+The device error word must stay clear (no pipeline wait expired)."""
+import numpy as np
+import pytest
+
+from oracle.ops import rel_fro
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(128, 128, 64), (128, 256, 128), (256, 512, 320), (129, 257, 100), (1, 300, 7), (300, 1, 513),
+          (1000, 1000, 1000), (64, 2048, 8)]
+
+
+@pytest.fixture(scope="module")
+def vk():
+    import vulkpy_gb300
+    return vulkpy_gb300
+
+
+@pytest.mark.parametrize("m,n,k", SHAPES)
+@pytest.mark.parametrize("prec,bound", [("bf16", 8e-3), ("bf16x3", 1e-5)])
+def test_tc_matmul_accuracy(gpu, vk, m, n, k, prec, bound):
+    gpu.check_errors()
+    rng = np.random.default_rng(m * 7 + n * 13 + k)
+    a = rng.standard_normal((m, k)).astype(np.float32)
+    b = rng.standard_normal((k, n)).astype(np.float32)
+    got = np.asarray(vk.vkarray.matmul(vk.Array(gpu, data=a), vk.Array(gpu, data=b), precision=prec))
+    assert gpu.check_errors() == 0
+    err = rel_fro(got, a.astype(np.float64) @ b.astype(np.float64))
+    assert err < bound, (prec, m, n, k, err)
+
+
+@pytest.mark.parametrize("ta,tb", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_tc_gemm_transposes_alpha_beta(gpu, vk, ta, tb):
+    """vkc_gemm through the C ABI with transposed operands, alpha and beta."""
+    import ctypes as C
+    from vulkpy_gb300 import _lib
+    rng = np.random.default_rng(ta * 2 + tb)
+    M, N, K = 200, 136, 72
+    A = rng.standard_normal((K, M) if ta else (M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K) if tb else (K, N)).astype(np.float32)
+    C0 = rng.standard_normal((M, N)).astype(np.float32)
+    a, b, c = vk.Array(gpu, data=A), vk.Array(gpu, data=B), vk.Array(gpu, data=C0)
+    st = _lib.lib.vkc_gemm(gpu.handle, _lib.MM_BF16X3, ta, tb, M, N, K, C.c_float(0.5), a._dptr(), A.shape[1],
+                           b._dptr(), B.shape[1], C.c_float(2.0), c._dptr(), N)
+    assert st == 0, _lib.last_error()
+    c._written()
+    opA = A.T if ta else A
+    opB = B.T if tb else B
+    exp = 0.5 * (opA.astype(np.float64) @ opB) + 2.0 * C0
+    assert rel_fro(np.asarray(c), exp) < 1e-5
+    assert gpu.check_errors() == 0
+
+
+def test_dense_layer_on_tensor_cores(gpu, vk):
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((256, 784)).astype(np.float32)
+    W = (rng.standard_normal((1024, 784)) * 0.05).astype(np.float32)
+    bvec = rng.standard_normal(1024).astype(np.float32)
+    old = gpu.matmul_precision
+    gpu.matmul_precision = "bf16x3"
+    try:
+        d = vk.nn.Dense(gpu, 784, 1024, w_init=lambda g, s: vk.Array(g, data=W),
+                        b_init=lambda g, s: vk.Array(g, data=bvec))
+        y = np.asarray(d(vk.Array(gpu, data=x)))
+        dy = rng.standard_normal((256, 1024)).astype(np.float32)
+        dx = np.asarray(d.backward(vk.Array(gpu, data=dy)))
+        dW = np.asarray(d.w.grad)
+    finally:
+        gpu.matmul_precision = old
+    x64 = x.astype(np.float64)
+    assert rel_fro(y, x64 @ W.T.astype(np.float64) + bvec) < 1e-5
+    assert rel_fro(dx, dy.astype(np.float64) @ W.astype(np.float64)) < 1e-5
+    assert rel_fro(dW, dy.astype(np.float64).T @ x64) < 1e-5
+    assert gpu.check_errors() == 0

@@ -1,11 +1,413 @@
-// Tensor-core GEMM (tcgen05).  Not built yet: reports an error.
+// Tensor-core GEMM for sm_103a: TMA -> 128B-swizzled shared memory ->
+// tcgen05.mma (bf16 x bf16, fp32 accumulate in TMEM) -> tcgen05.ld epilogue.
+//
+// C[M,N] = act(alpha * op(A) op(B) + beta * C + bias), A/B/C fp32 in memory.
+// A pre-pass turns op(A) (M x K) and op(B)^T (N x K) into K-major bf16
+// copies: x ~ hi = bf16(x) and, for the split mode, lo = bf16(x - hi).  The
+// split-bf16x3 product accumulates hi*hi + hi*lo + lo*hi per K step, which
+// keeps ~16 significant bits per operand (relative representation error
+// <= 2^-17) at three tensor-core products instead of fp32 FMA.
+//
+// One CTA computes a 128 x BN tile with 6 warps:
+//   warp 0 lane 0  TMA producer: STAGES-deep ring of (A, B[, A_lo, B_lo]) tiles
+//   warp 1         allocates TMEM; lane 0 issues tcgen05.mma and commits
+//   warps 2-5      epilogue: tcgen05.ld 32 columns at a time, alpha/beta/bias/act
+// Every mbarrier wait is bounded by a wall-clock limit; on expiry the CTA
+// records bit1 in the device error word, drains what it issued and returns.
 #include "gemm_tc.cuh"
 
-namespace vkc {
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
 
-int gemm_tc(vkc_device_t, int precision, bool, bool, int64_t, int64_t, int64_t, float, const float*, int64_t,
-            const float*, int64_t, float, float*, int64_t, GemmEpilogue) {
-  return set_error(VKC_ERR_INVALID, "matmul precision %d (tensor cores) is not available in this build", precision);
+#include <algorithm>
+#include <mutex>
+
+namespace vkc {
+namespace {
+
+constexpr int kBM = 128;
+constexpr int kBK = 64;                       // 64 bf16 = one 128-byte swizzle row
+constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s per wait
+constexpr int kThreadsTC = 192;
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the phase of `bar` with parity `parity`; false after the limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitTimeoutNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, K-major with 128-byte swizzle: 8-row
+// groups 1024 bytes apart (stride byte offset), version 1, layout 2.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);   // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)2 << 61;                    // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 lanes x 32 consecutive 32-bit columns: thread i of the warp gets lane
+// (taddr.lane + i), columns taddr.col .. +31.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// ------------------------------------------------------------ the kernel
+template <int BN, bool X3, int STAGES>
+struct TcCfg {
+  static constexpr uint32_t kABytes = kBM * kBK * 2;
+  static constexpr uint32_t kBBytes = BN * kBK * 2;
+  static constexpr uint32_t kStageBytes = (X3 ? 2u : 1u) * (kABytes + kBBytes);
+  static constexpr uint32_t kSmem = STAGES * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+  static constexpr uint32_t kTmemCols = BN;  // fp32 accumulator: one column per output column
+};
+
+template <int BN, bool X3, int STAGES>
+__global__ void __launch_bounds__(kThreadsTC, 1)
+k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+          const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N, int K,
+          float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
+          uint32_t* err) {
+  using Cfg = TcCfg<BN, X3, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* gbase = smem_raw + (base - raw);
+  const uint32_t bars = base + STAGES * Cfg::kStageBytes;
+  auto full_bar = [&](int s) { return bars + 8u * s; };
+  auto empty_bar = [&](int s) { return bars + 8u * (STAGES + s); };
+  const uint32_t acc_bar = bars + 16u * STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * Cfg::kStageBytes + 16 * STAGES + 8);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
+  const int nk = (K + kBK - 1) / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    mbar_init(acc_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(Cfg::kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
+
+  auto stage_a = [&](int s) { return base + s * Cfg::kStageBytes; };
+  auto stage_b = [&](int s) { return stage_a(s) + Cfg::kABytes; };
+  auto stage_alo = [&](int s) { return stage_b(s) + Cfg::kBBytes; };
+  auto stage_blo = [&](int s) { return stage_alo(s) + Cfg::kABytes; };
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int issued = 0;
+    bool ok = true;
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (*abort_flag || !mbar_wait(empty_bar(s), ph ^ 1)) { ok = false; break; }
+      mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
+      tma_load_2d(stage_a(s), &map_a, full_bar(s), kb * kBK, m0);
+      tma_load_2d(stage_b(s), &map_b, full_bar(s), kb * kBK, n0);
+      if (X3) {
+        tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kb * kBK, m0);
+        tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kb * kBK, n0);
+      }
+      ++issued;
+    }
+    if (!ok) {
+      atomicOr(err, 2u);
+      *abort_flag = 1;
+      // drain the copies still in flight into this CTA's shared memory
+      for (int kb = std::max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    constexpr uint32_t idesc = (1u << 4)            // D: fp32
+                               | (1u << 7)          // A: bf16
+                               | (1u << 10)         // B: bf16
+                               | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+    bool ok = true;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (*abort_flag || !mbar_wait(full_bar(s), ph)) { ok = false; break; }
+      tc_fence_after();
+#pragma unroll
+      for (int k = 0; k < kBK / 16; ++k) {
+        const uint64_t a = sw128_desc(stage_a(s) + 32u * k);
+        const uint64_t b = sw128_desc(stage_b(s) + 32u * k);
+        mma_bf16(tmem, a, b, idesc, (kb | k) != 0);
+        if (X3) {
+          mma_bf16(tmem, a, sw128_desc(stage_blo(s) + 32u * k), idesc, 1);
+          mma_bf16(tmem, sw128_desc(stage_alo(s) + 32u * k), b, idesc, 1);
+        }
+      }
+      mma_commit(empty_bar(s));  // frees the stage once these MMAs have read it
+    }
+    if (!ok) {
+      atomicOr(err, 2u);
+      *abort_flag = 1;
+    }
+    mma_commit(acc_bar);  // fires when every MMA issued above has completed
+  } else if (warp >= 2) {
+    // ---------------- epilogue: TMEM -> registers -> global
+    const bool ok = mbar_wait(acc_bar, 0) && !*abort_flag && nk > 0;
+    tc_fence_after();
+    const int q = warp & 3;  // TMEM lanes 32q .. 32q+31 belong to this warp
+    const int row = m0 + q * 32 + lane;
+    if (!ok) {
+      if (lane == 0) atomicOr(err, 2u);
+    } else {
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), r);
+        if (row < M) {
+          float* crow = C + (int64_t)row * ldc;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = n0 + c * 32 + j;
+            if (col < N) {
+              float v = alpha * __uint_as_float(r[j]);
+              if (beta != 0.f) v += beta * crow[col];
+              if (bias) v += bias[col];
+              if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+              else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+              crow[col] = v;
+            }
+          }
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols) : "memory");
+  }
+}
+
+// ------------------------------------------------------------ operand split
+// K contiguous in the source: dst[r*Kp + k] from src[r*ld + k]; zero padding k >= K.
+__global__ void k_split_kmajor(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
+                               __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+  const int64_t total = R * Kp;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const int64_t r = i / Kp, k = i - r * Kp;
+    const float x = k < K ? src[r * ld + k] : 0.f;
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    hi[i] = h;
+    if (lo) lo[i] = __float2bfloat16_rn(x - __bfloat162float(h));
+  }
+}
+
+// K is the row index of the source (src[k*ld + r]): 32x32 tiles through
+// shared memory so both the read and the write are coalesced.
+__global__ void k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
+                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+  __shared__ float tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int j = ty; j < 32; j += 8) {
+    const int64_t k = k0 + j, r = r0 + tx;
+    tile[j][tx] = (k < K && r < R) ? src[k * ld + r] : 0.f;
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int64_t r = r0 + j, k = k0 + tx;
+    if (r < R && k < Kp) {
+      const float x = tile[tx][j];
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      hi[r * Kp + k] = h;
+      if (lo) lo[r * Kp + k] = __float2bfloat16_rn(x - __bfloat162float(h));
+    }
+  }
+}
+
+// Produce K-major bf16 copies of a logical (R x K) operand.  `k_contig`:
+// element (r, k) is src[r*ld + k]; otherwise src[k*ld + r].
+int split_operand(vkc_device_t dev, const float* src, int64_t R, int64_t K, int64_t ld, bool k_contig,
+                  __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t Kp) {
+  if (k_contig) {
+    unsigned grid = stream_grid(dev, (size_t)(R * Kp), 256);
+    k_split_kmajor<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
+  } else {
+    dim3 grid((unsigned)((R + 31) / 32), (unsigned)((Kp + 31) / 32));
+    if (grid.y > 65535) return set_error(VKC_ERR_INVALID, "matmul: K too large for the transpose pre-pass");
+    k_split_transpose<<<grid, dim3(32, 8), 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
+  }
+  return check_launch("split_operand");
+}
+
+// ------------------------------------------------------------ host side
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// 2-D bf16 map over [rows][Kp] with a (64 x box_rows) box and 128B swizzle.
+int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t Kp, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return set_error(VKC_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(Kp * 2)};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(VKC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return VKC_OK;
+}
+
+template <int BN, bool X3, int STAGES>
+int launch_tc(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
+              const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C, int64_t ldc,
+              const GemmEpilogue& epi) {
+  using Cfg = TcCfg<BN, X3, STAGES>;
+  auto kern = k_gemm_tc<BN, X3, STAGES>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    VKC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
+    attr_set = true;
+  }
+  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + kBM - 1) / kBM));
+  kern<<<grid, kThreadsTC, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
+                                                      epi.bias, epi.act, dev->err_word);
+  return check_launch("gemm_tc");
+}
+
+}  // namespace
+
+int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
+            const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+            GemmEpilogue epi) {
+  if (M == 0 || N == 0) return VKC_OK;
+  if (K == 0) return gemm_simt(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  VKC_REQUIRE(M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), "matmul dimension too large");
+  VKC_REQUIRE((M + kBM - 1) / kBM <= 65535, "matmul: M too large for the tensor-core grid");
+  const bool x3 = precision == VKC_MM_BF16X3;
+  const int64_t Kp = (K + 7) / 8 * 8;  // 16-byte aligned rows for TMA
+  const size_t a_elems = (size_t)M * Kp, b_elems = (size_t)N * Kp;
+  const size_t bytes = (a_elems + b_elems) * sizeof(__nv_bfloat16) * (x3 ? 2 : 1);
+  void* scratch = nullptr;
+  int r = scratch_alloc(dev, bytes, &scratch);
+  if (r != VKC_OK) return r;
+  auto* a_hi = static_cast<__nv_bfloat16*>(scratch);
+  auto* b_hi = a_hi + a_elems;
+  __nv_bfloat16* a_lo = x3 ? b_hi + b_elems : nullptr;
+  __nv_bfloat16* b_lo = x3 ? a_lo + a_elems : nullptr;
+  // op(A)(m,k): ta ? A[k*lda + m] : A[m*lda + k]  -> K contiguous iff !ta
+  // op(B)(k,n): tb ? B[n*ldb + k] : B[k*ldb + n]  -> (n,k) K contiguous iff tb
+  r = split_operand(dev, A, M, K, lda, !ta, a_hi, a_lo, Kp);
+  if (r == VKC_OK) r = split_operand(dev, B, N, K, ldb, tb, b_hi, b_lo, Kp);
+  CUtensorMap ma, mb, malo, mblo;
+  const int bn = x3 ? 128 : 256;
+  if (r == VKC_OK) r = make_map(&ma, a_hi, M, Kp, kBM);
+  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, bn);
+  if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
+  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, bn);
+  if (r == VKC_OK) {
+    if (x3) r = launch_tc<128, true, 3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
+    else r = launch_tc<256, false, 4>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
+  }
+  scratch_free(dev, scratch);
+  return r;
 }
 
 }  // namespace vkc

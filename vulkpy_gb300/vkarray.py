@@ -794,6 +794,22 @@ class Array(_GPUArray):
         return ret
 
 
+def matmul(a: Array, b: Array, precision: Optional[str] = None) -> Array:
+    """``a @ b`` with an explicit arithmetic: "fp32" (SIMT FMA, the drop-in
+    default), "bf16" (tensor cores, fp32 accumulate) or "bf16x3" (split
+    bf16 on tensor cores: ~fp32 accuracy, relative error ~1e-6..1e-5)."""
+    if precision is None:
+        return a @ b
+    old = a._gpu.matmul_precision
+    if precision not in _MATMUL_PRECISION:
+        raise ValueError(f"unknown matmul precision {precision!r}")
+    a._gpu.matmul_precision = precision
+    try:
+        return a @ b
+    finally:
+        a._gpu.matmul_precision = old
+
+
 def _pad(shape, nd) -> tuple:
     shape = tuple(int(s) for s in shape)
     return (1,) * (nd - len(shape)) + shape
