@@ -183,6 +183,17 @@ int vkc_broadcast_to(vkc_device_t dev, const float* a, const int64_t* a_shape,
  * vkarray.py:1246-1274 (axis=None), sum.comp:18-30, sum_v1.3.comp:20-29. */
 int vkc_reduce_all(vkc_device_t dev, int op, int precision, const float* a, size_t n,
                    float* out, float scale);
+/* Same result contract as vkc_reduce_all, for callers that cannot allocate
+ * device memory during the call (a host that hands the whole device heap to
+ * its own allocator, or a latency-critical path where an allocation could
+ * block or fail).  No counterpart in the reference.  The block partials
+ * live in a fixed 1 MiB device array inside the library, so n is limited to
+ * 2^29 elements (larger n: VKC_ERR_INVALID).  The first call on a device
+ * looks the array up (make it before capturing the stream); calls on one
+ * device share the array, so calls that overlap on the GPU race.  Allocates
+ * nothing: no cudaMalloc/cudaFree, no pool. */
+int vkc_reduce_all_noalloc(vkc_device_t dev, int op, int precision, const float* a, size_t n,
+                           float* out, float scale);
 /* View a as [prev, axis, post]; out[i, j] = reduce_k a[i, k, j] * scale.
  * With rebroadcast != 0, out has a's shape and every k gets the result.
  * vkarray.py:1194-1244, sum_axis.comp:20-32, sum_axis_rebroadcast.comp:20-35. */

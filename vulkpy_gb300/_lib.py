@@ -80,6 +80,7 @@ _SIGS = {
     "vkc_broadcast_to": ([vp, vp, pi64, vp, pi64, i32], i32),
     "vkc_reduce_all": ([vp, i32, i32, vp, sz, vp, f32], i32),
     "vkc_reduce_axis": ([vp, i32, vp, sz, sz, sz, vp, i32, f32], i32),
+    "vkc_reduce_all_noalloc": ([vp, i32, i32, vp, sz, vp, f32], i32),
     "vkc_matmul": ([vp, i32, vp, vp, vp, i64, i64, i64], i32),
     "vkc_gemm": ([vp, i32, i32, i32, i64, i64, i64, f32, vp, i64, vp, i64, f32, vp, i64], i32),
     "vkc_gather": ([vp, vp, sz, vp, sz, vp], i32),

@@ -521,3 +521,94 @@ VKC_EXPORT int vkc_reduce_axis(vkc_device_t dev, int op, const float* a, size_t 
     default: return vkc::set_error(VKC_ERR_INVALID, "unknown reduce op %d", op);
   }
 }
+
+// ------------------------------------------------------- allocation-free variant
+//
+// vkc_reduce_all_noalloc is vkc_reduce_all for callers that cannot allocate
+// device memory at call time: hosts that hand the whole device heap to their
+// own allocator up front (so a stream-ordered allocation here could fail or
+// be refused), and latency-critical paths where an allocation's possible
+// synchronisation or failure is not acceptable.  The block partials that
+// vkc_reduce_all takes from the memory pool live instead in a file-scope
+// device array of fixed size (1 MiB, 65536 partials), so one call handles at
+// most 65536 * 8192 = 2^29 elements and rejects larger inputs.  Every GPU
+// that loads this library holds the array until the process exits.
+//
+// Set-up: the first call on each device, with that device current, looks up
+// the array's device address (cudaGetSymbolAddress) and caches it; make that
+// first call before capturing the stream.  All calls on a device share the
+// one array and it keeps the previous call's contents: each block overwrites
+// its own slot before the combine kernel reads it, so nothing has to start at
+// zero, but calls that overlap on the GPU (different streams, or different
+// threads without ordering) race on it.
+namespace {
+
+constexpr size_t kNoAllocPerBlock = (size_t)kThreads * 4 * 8;  // elements per block partial
+constexpr size_t kNoAllocMaxPartials = 65536;
+constexpr size_t kNoAllocMaxElements = kNoAllocPerBlock * kNoAllocMaxPartials;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_partials[2 * kNoAllocMaxPartials];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+int noalloc_partials(vkc_device_t dev, double** out) {
+  VKC_REQUIRE(dev->index >= 0 && dev->index < kNoAllocMaxDevices, "device index %d not supported", dev->index);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev->index]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess || !p)
+      return vkc::set_error(VKC_ERR_CUDA, "cudaGetSymbolAddress(no-alloc partials): %s", cudaGetErrorString(e));
+    g_noalloc_addr[dev->index] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[dev->index];
+  return VKC_OK;
+}
+
+template <int OP, bool COMP, int NACC>
+int reduce_all_noalloc_impl(vkc_device_t dev, const float* a, size_t n, float* out, float scale, double* partials) {
+  const size_t grid = (n + kNoAllocPerBlock - 1) / kNoAllocPerBlock;
+  if (grid == 1) {
+    k_reduce_all<OP, COMP, NACC><<<1, kThreads, 0, dev->stream>>>(a, n, nullptr, out, scale);
+    return vkc::check_launch("reduce_all_noalloc");
+  }
+  k_reduce_all<OP, COMP, NACC><<<(unsigned)grid, kThreads, 0, dev->stream>>>(a, n, partials, out, scale);
+  int r = vkc::check_launch("reduce_all_noalloc");
+  if (r != VKC_OK) return r;
+  const bool fp64 = (OP == VKC_SUM || OP == VKC_PROD) && n >= (size_t(1) << 24);
+  if (fp64) k_reduce_partials<OP, COMP, true><<<1, 1024, 0, dev->stream>>>(partials, (int)grid, out, scale);
+  else k_reduce_partials<OP, COMP, false><<<1, 1024, 0, dev->stream>>>(partials, (int)grid, out, scale);
+  return vkc::check_launch("reduce_partials_noalloc");
+}
+
+}  // namespace
+
+VKC_EXPORT int vkc_reduce_all_noalloc(vkc_device_t dev, int op, int precision, const float* a, size_t n, float* out,
+                                      float scale) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(a && out, "NULL buffer");
+  VKC_REQUIRE(n > 0, "reduction of an empty array");
+  VKC_REQUIRE(n <= kNoAllocMaxElements,
+              "vkc_reduce_all_noalloc: %zu elements exceed the maximum of %zu (fixed 1 MiB scratch); "
+              "use vkc_reduce_all", n, kNoAllocMaxElements);
+  VKC_REQUIRE(((uintptr_t)a & 15u) == 0, "reduce: input must be 16-byte aligned");
+  VKC_REQUIRE(precision >= VKC_RED_PLAIN && precision <= VKC_RED_COMPENSATED, "bad precision %d", precision);
+  double* partials = nullptr;
+  int r = noalloc_partials(dev, &partials);
+  if (r != VKC_OK) return r;
+  switch (op) {
+    case VKC_SUM:
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_noalloc_impl<VKC_SUM, true, 1>(dev, a, n, out, scale, partials);
+      if (precision == VKC_RED_PAIRWISE) return reduce_all_noalloc_impl<VKC_SUM, false, 16>(dev, a, n, out, scale, partials);
+      return reduce_all_noalloc_impl<VKC_SUM, false, 1>(dev, a, n, out, scale, partials);
+    case VKC_PROD:
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_noalloc_impl<VKC_PROD, true, 1>(dev, a, n, out, scale, partials);
+      if (precision == VKC_RED_PAIRWISE) return reduce_all_noalloc_impl<VKC_PROD, false, 16>(dev, a, n, out, scale, partials);
+      return reduce_all_noalloc_impl<VKC_PROD, false, 1>(dev, a, n, out, scale, partials);
+    case VKC_MAXIMUM: return reduce_all_noalloc_impl<VKC_MAXIMUM, false, 1>(dev, a, n, out, scale, partials);
+    case VKC_MINIMUM: return reduce_all_noalloc_impl<VKC_MINIMUM, false, 1>(dev, a, n, out, scale, partials);
+    default: return vkc::set_error(VKC_ERR_INVALID, "unknown reduce op %d", op);
+  }
+}
