@@ -245,6 +245,11 @@ def gpu_arm(args, rank, world, dist):
     breakdown = profile_ops(vk, gpu, timer, X, row, col, idx, rng, U, Nrm, I)
 
     e2e = e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, dist)
+    del X, U, Nrm, I, idx
+    extra = {}
+    if not args.no_extra:
+        extra["matmul"] = matmul_study(vk, gpu, timer)
+        extra["mlp"] = mlp_study(vk, gpu, timer)
 
     result = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -257,6 +262,7 @@ def gpu_arm(args, rank, world, dist):
                    "parallelism": f"replicas x{world}"},
         "roofline": roofline, "e2e": e2e, "clocks": clk, "gpu_launches": launches, "ops_gbs": breakdown,
     }
+    result.update(extra)
     return result
 
 
@@ -334,6 +340,80 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, np.asarray)"}
+
+
+# ---------------------------------------------------------------- matmul / MLP
+def matmul_study(vk, gpu, timer, sizes=(4096, 8192)):
+    """C = A @ B, A, B ~ N(0,1) fp32 (seed 0), in fp32 SIMT, bf16 and split
+    bf16x3 on tensor cores: TFLOP/s (2MNK / CUDA-event time) and relative
+    Frobenius error vs float64 over the first 128 rows of C."""
+    out = {}
+    for n in sizes:
+        rng = np.random.default_rng(0)
+        A = rng.standard_normal((n, n), dtype=np.float32)
+        B = rng.standard_normal((n, n), dtype=np.float32)
+        ref = A[:128].astype(np.float64) @ B.astype(np.float64)
+        a, b = vk.Array(gpu, data=A), vk.Array(gpu, data=B)
+        for prec in ("fp32", "bf16", "bf16x3"):
+            c = vk.vkarray.matmul(a, b, precision=prec)
+            gpu.wait()
+            reps = 3 if (prec == "fp32" and n >= 8192) else 10
+            t0 = timer.mark()
+            for _ in range(reps):
+                c = vk.vkarray.matmul(a, b, precision=prec)
+            t1 = timer.mark()
+            gpu.wait()
+            ms = timer.ms(t0, t1) / reps
+            timer.free(t0, t1)
+            err = float(np.linalg.norm(np.asarray(c)[:128] - ref) / np.linalg.norm(ref))
+            out[f"{prec}_{n}"] = {"tflops": round(2 * n ** 3 / (ms * 1e-3) / 1e12, 1), "ms": round(ms, 3),
+                                  "rel_err_fp64": float(f"{err:.3g}")}
+        del a, b, c
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = json.load(open(peaks_path))["bf16_tflops"] if os.path.exists(peaks_path) else 1900.0
+    best = out.get(f"bf16x3_{sizes[-1]}", {}).get("tflops")
+    return {"unit": "TFLOP/s (2MNK)", "results": out, "bf16_peak_tflops": peak,
+            "bf16x3_vs_fp32_speedup": round(best / out[f"fp32_{sizes[-1]}"]["tflops"], 2) if best else None,
+            "note": "bf16x3 issues 3 tensor products per K step; TFLOP/s counts the algorithmic 2MNK"}
+
+
+def mlp_study(vk, gpu, timer, steps=50):
+    """One Sequence.train step of Dense 784-1024, ReLU, Dense 1024-1024,
+    Sigmoid, Dense 1024-10, softmax cross entropy, Adam(1e-3), batch 256,
+    HeNormal(seed 1); steps/s for fp32 SIMT vs split-bf16x3 matmuls."""
+    nn = vk.nn
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((256, 784)).astype(np.float32)
+    Y = np.eye(10, dtype=np.float32)[rng.integers(0, 10, 256)]
+    res = {}
+    for prec in ("fp32", "bf16x3"):
+        gpu.matmul_precision = prec
+        opt = nn.Adam(gpu, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8)
+        net = nn.Sequence([
+            nn.Dense(gpu, 784, 1024, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 784, seed=1)),
+            nn.ReLU(),
+            nn.Dense(gpu, 1024, 1024, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 1024, seed=1)),
+            nn.Sigmoid(),
+            nn.Dense(gpu, 1024, 10, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 1024, seed=1)),
+        ], nn.SoftmaxCrossEntropyLoss())
+        x, y = vk.Array(gpu, data=X), vk.Array(gpu, data=Y)
+        for _ in range(5):
+            net.train(x, y)
+        gpu.wait()
+        t0 = timer.mark()
+        for _ in range(steps):
+            _, loss = net.train(x, y)
+        t1 = timer.mark()
+        gpu.wait()
+        ms = timer.ms(t0, t1) / steps
+        timer.free(t0, t1)
+        res[prec] = {"steps_per_s": round(1000.0 / ms, 1), "ms_per_step": round(ms, 4),
+                     "loss_after": float(np.asarray(loss)[0])}
+    gpu.matmul_precision = "fp32"
+    flop = 3 * 2 * 256 * (784 * 1024 + 1024 * 1024 + 1024 * 10)
+    res["flop_per_step"] = flop
+    res["speedup_bf16x3_vs_fp32"] = round(res["bf16x3"]["steps_per_s"] / res["fp32"]["steps_per_s"], 2)
+    return res
 
 
 # ---------------------------------------------------------------- CPU oracle
@@ -465,6 +545,7 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=256)
     ap.add_argument("--cpu-passes", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the matmul and MLP studies")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

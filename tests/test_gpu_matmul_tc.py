@@ -13,7 +13,7 @@ from oracle.ops import rel_fro
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(128, 128, 64), (128, 256, 128), (256, 512, 320), (129, 257, 100), (1, 300, 7), (300, 1, 513),
-          (1000, 1000, 1000), (64, 2048, 8)]
+          (1000, 1000, 1000), (64, 2048, 8), (256, 384, 4096), (512, 512, 8192)]
 
 
 @pytest.fixture(scope="module")

@@ -272,6 +272,192 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
   }
 }
 
+// ------------------------------------------------------------ split-bf16x3
+// The tensor core adds each MMA's result into the fp32 TMEM accumulator
+// with truncation, so the error of one long accumulation grows with K/16
+// (measured: 1.5e-5 relative at K = 4096, 2.9e-5 at 8192).  This kernel
+// restarts the accumulation every 64-wide K block in one of kAccBufs TMEM
+// buffers and the epilogue warps add each block's partial into fp32
+// registers with round-to-nearest, overlapping with the next blocks' MMAs.
+constexpr int kAccBufs = 4;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+template <int STAGES>
+__global__ void __launch_bounds__(kThreadsTC, 1)
+k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+             const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
+             int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
+             uint32_t* err) {
+  constexpr int BN = 128;
+  using Cfg = TcCfg<BN, true, STAGES>;
+  constexpr uint32_t kCols = BN * kAccBufs;  // 512: all of TMEM
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* gbase = smem_raw + (base - raw);
+  const uint32_t bars = base + STAGES * Cfg::kStageBytes;
+  auto full_bar = [&](int s) { return bars + 8u * s; };
+  auto empty_bar = [&](int s) { return bars + 8u * (STAGES + s); };
+  auto accf_bar = [&](int b) { return bars + 8u * (2 * STAGES + b); };
+  auto acce_bar = [&](int b) { return bars + 8u * (2 * STAGES + kAccBufs + b); };
+  const uint32_t drain_bar = bars + 8u * (2 * STAGES + 2 * kAccBufs);
+  uint32_t* tmem_slot =
+      reinterpret_cast<uint32_t*>(gbase + STAGES * Cfg::kStageBytes + 8 * (2 * STAGES + 2 * kAccBufs + 1));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
+  const int nk = (K + kBK - 1) / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < kAccBufs; ++b) {
+      mbar_init(accf_bar(b), 1);
+      mbar_init(acce_bar(b), 4);  // one arrive per epilogue warp
+    }
+    mbar_init(drain_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
+
+  auto stage_a = [&](int s) { return base + s * Cfg::kStageBytes; };
+  auto stage_b = [&](int s) { return stage_a(s) + Cfg::kABytes; };
+  auto stage_alo = [&](int s) { return stage_b(s) + Cfg::kBBytes; };
+  auto stage_blo = [&](int s) { return stage_alo(s) + Cfg::kABytes; };
+
+  if (warp == 0 && lane == 0) {
+    int issued = 0;
+    bool ok = true;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      if (*abort_flag || !mbar_wait(empty_bar(s), ((kb / STAGES) & 1) ^ 1)) { ok = false; break; }
+      mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
+      tma_load_2d(stage_a(s), &map_a, full_bar(s), kb * kBK, m0);
+      tma_load_2d(stage_b(s), &map_b, full_bar(s), kb * kBK, n0);
+      tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kb * kBK, m0);
+      tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kb * kBK, n0);
+      ++issued;
+    }
+    if (!ok) {
+      atomicOr(err, 2u);
+      *abort_flag = 1;
+      for (int kb = std::max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                               ((uint32_t)(kBM >> 4) << 24);
+    bool ok = true;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES, b = kb % kAccBufs;
+      if (*abort_flag || !mbar_wait(full_bar(s), (kb / STAGES) & 1) ||
+          !mbar_wait(acce_bar(b), ((kb / kAccBufs) & 1) ^ 1)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + (uint32_t)(b * BN);
+#pragma unroll
+      for (int k = 0; k < kBK / 16; ++k) {
+        const uint64_t a = sw128_desc(stage_a(s) + 32u * k);
+        const uint64_t bb = sw128_desc(stage_b(s) + 32u * k);
+        // small cross terms first, the dominant hi*hi term last
+        mma_bf16(d, a, sw128_desc(stage_blo(s) + 32u * k), idesc, k != 0);
+        mma_bf16(d, sw128_desc(stage_alo(s) + 32u * k), bb, idesc, 1);
+        mma_bf16(d, a, bb, idesc, 1);
+      }
+      mma_commit(empty_bar(s));
+      mma_commit(accf_bar(b));
+    }
+    if (!ok) {
+      atomicOr(err, 2u);
+      *abort_flag = 1;
+    }
+  } else if (warp >= 2) {
+    const int q = warp & 3;
+    const int row = m0 + q * 32 + lane;
+    float sum[BN];
+#pragma unroll
+    for (int j = 0; j < BN; ++j) sum[j] = 0.f;
+    bool ok = nk > 0;
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int b = kb % kAccBufs;
+      if (*abort_flag || !mbar_wait(accf_bar(b), (kb / kAccBufs) & 1)) { ok = false; break; }
+      tc_fence_after();
+#pragma unroll
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c * 32), r);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) sum[c * 32 + j] += __uint_as_float(r[j]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce_bar(b));
+    }
+    if (!ok) {
+      if (lane == 0) atomicOr(err, 2u);
+      *abort_flag = 1;
+    } else {
+      // All MMAs are done, so the operand stages are free: stage this warp's
+      // 32 x 128 block in shared memory (row pitch 129 floats: conflict-free
+      // both ways) and write it back one coalesced 128-float row at a time.
+      float* tile = reinterpret_cast<float*>(gbase) + q * 32 * (BN + 1);
+#pragma unroll
+      for (int j = 0; j < BN; ++j) tile[lane * (BN + 1) + j] = sum[j];
+      __syncwarp();
+      for (int rr = 0; rr < 32; ++rr) {
+        const int grow = m0 + q * 32 + rr;
+        if (grow >= M) break;
+        float* crow = C + (int64_t)grow * ldc;
+#pragma unroll
+        for (int i = 0; i < BN / 32; ++i) {
+          const int j = i * 32 + lane;
+          const int col = n0 + j;
+          if (col < N) {
+            float v = alpha * tile[rr * (BN + 1) + j];
+            if (beta != 0.f) v += beta * crow[col];
+            if (bias) v += bias[col];
+            if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+            else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+            crow[col] = v;
+          }
+        }
+      }
+      (void)row;
+    }
+  }
+
+  // Before TMEM is released every MMA must have completed.  On the normal
+  // path the epilogue waited for the last block's commit; after an abort the
+  // issuer commits once more and waits (bounded) for that.
+  if (warp == 1 && lane == 0 && *abort_flag) {
+    mma_commit(drain_bar);
+    mbar_wait(drain_bar, 0);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+  }
+}
+
 // ------------------------------------------------------------ operand split
 // K contiguous in the source: dst[r*Kp + k] from src[r*ld + k]; zero padding k >= K.
 __global__ void k_split_kmajor(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
@@ -372,6 +558,23 @@ int launch_tc(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, co
   return check_launch("gemm_tc");
 }
 
+template <int STAGES>
+int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
+                 const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C,
+                 int64_t ldc, const GemmEpilogue& epi) {
+  using Cfg = TcCfg<128, true, STAGES>;
+  auto kern = k_gemm_tc_x3<STAGES>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    VKC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
+    attr_set = true;
+  }
+  dim3 grid((unsigned)((N + 127) / 128), (unsigned)((M + kBM - 1) / kBM));
+  kern<<<grid, kThreadsTC, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
+                                                      epi.bias, epi.act, dev->err_word);
+  return check_launch("gemm_tc_x3");
+}
+
 }  // namespace
 
 int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
@@ -403,7 +606,7 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
   if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, bn);
   if (r == VKC_OK) {
-    if (x3) r = launch_tc<128, true, 3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
+    if (x3) r = launch_tc_x3<3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
     else r = launch_tc<256, false, 4>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
   }
   scratch_free(dev, scratch);
