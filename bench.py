@@ -408,11 +408,29 @@ def mlp_study(vk, gpu, timer, steps=50):
         ms = timer.ms(t0, t1) / steps
         timer.free(t0, t1)
         res[prec] = {"steps_per_s": round(1000.0 / ms, 1), "ms_per_step": round(ms, 4),
-                     "loss_after": float(np.asarray(loss)[0])}
+                     "loss_after": float(np.asarray(loss))}
+        # the same step captured once as a CUDA graph and replayed
+        step = net.compile(x, y)
+        for _ in range(3):
+            step()
+        gpu.wait()
+        t0 = timer.mark()
+        for _ in range(steps * 4):
+            _, loss = step()
+        t1 = timer.mark()
+        gpu.wait()
+        ms = timer.ms(t0, t1) / (steps * 4)
+        timer.free(t0, t1)
+        res[prec + "_graph"] = {"steps_per_s": round(1000.0 / ms, 1), "ms_per_step": round(ms, 4),
+                                "loss_after": float(np.asarray(loss))}
+        del step, net, opt
     gpu.matmul_precision = "fp32"
     flop = 3 * 2 * 256 * (784 * 1024 + 1024 * 1024 + 1024 * 10)
     res["flop_per_step"] = flop
-    res["speedup_bf16x3_vs_fp32"] = round(res["bf16x3"]["steps_per_s"] / res["fp32"]["steps_per_s"], 2)
+    res["speedup_bf16x3_graph_vs_fp32_eager"] = round(res["bf16x3_graph"]["steps_per_s"] /
+                                                      res["fp32"]["steps_per_s"], 2)
+    res["speedup_bf16x3_graph_vs_fp32_graph"] = round(res["bf16x3_graph"]["steps_per_s"] /
+                                                      res["fp32_graph"]["steps_per_s"], 2)
     return res
 
 

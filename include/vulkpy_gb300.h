@@ -144,6 +144,19 @@ int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms);
 /* Number of kernels this library has launched since load (all devices). */
 int vkc_launch_count(uint64_t* count);
 
+/* ---- CUDA graphs (no reference counterpart: vulkpy submits every op as
+ * its own Vulkan job, _vkarray.cc:403-438) ---------------------------------
+ * begin: start capturing the device's stream; every entry point called on
+ * this thread is recorded instead of run (stream-ordered allocations become
+ * graph memory nodes; uploads from the host are refused while capturing).
+ * end: stop and instantiate; allocations still live at the end are re-made
+ * at the same addresses on every launch.  launch: replay on the stream. */
+typedef struct vkc_graph* vkc_graph_t;
+int vkc_graph_begin(vkc_device_t dev);
+int vkc_graph_end(vkc_device_t dev, vkc_graph_t* graph);
+int vkc_graph_launch(vkc_graph_t graph);
+int vkc_graph_destroy(vkc_graph_t graph);
+
 /* ---- elementwise ---------------------------------- */
 /* c[i] = a[i] op b[i] for i < n; c may alias a or b (in-place i*.comp twins).
  * vulkpy/vkarray.py:440-452 (_opVec/_opVec3), shaders add.comp:20-26 etc. */
@@ -275,6 +288,21 @@ int vkc_cross_entropy(vkc_device_t dev, const float* x, const float* y, float* l
 int vkc_adam_update(vkc_device_t dev, float* value, const float* grad, float* m, float* v,
                     size_t n, double lr, double beta1, double beta2, double eps,
                     double beta1t, double beta2t);
+/* Adam with the running powers beta1^t, beta2^t kept on the device
+ * (`powers` = double[2], start at {1, 1}); the call multiplies them by
+ * beta1, beta2 first, exactly as AdamState.grad2diff does on the host, so a
+ * captured step can be replayed.  Same result as vkc_adam_update. */
+int vkc_adam_update_dev(vkc_device_t dev, float* value, const float* grad, float* m, float* v,
+                        size_t n, double lr, double beta1, double beta2, double eps, double* powers);
+/* dx = dy * f'(y) from the activation output y: ReLU dy * max(sign(y), 0)
+ * (layers.py:187-210); Sigmoid and Softmax (diagonal) (1 - y) * y * dy
+ * (layers.py:246-267, 302-323); same float32 op order as the reference. */
+int vkc_activation_backward(vkc_device_t dev, int act, const float* y, const float* dy, float* dx,
+                            size_t n);
+/* Softmax cross entropy gradient (p - y) * scale (losses.py:229-249 with the
+ * ReduceLoss scaling of losses.py:70-86); dx may alias p. */
+int vkc_softmax_ce_backward(vkc_device_t dev, const float* p, const float* y, float* dx, size_t n,
+                            float scale);
 /* value += (-lr) * grad (optimizers.py:39-52). */
 int vkc_sgd_update(vkc_device_t dev, float* value, const float* grad, size_t n, double lr);
 /* h += g^2; value += (g / (sqrt(h) + eps)) * (-lr)  (optimizers.py:120-139). */

@@ -103,3 +103,67 @@ def test_softmax_cross_entropy_rows(gpu, vk):
     np.testing.assert_allclose(np.asarray(sce.grad()), (p - y) / 300, rtol=1e-5, atol=1e-7)
     sm = vk.nn.Softmax()
     np.testing.assert_allclose(np.asarray(sm(vk.Array(gpu, data=x))), p, rtol=1e-5, atol=1e-7)
+
+
+def _mlp(vk, gpu, fuse=True, seed=3):
+    nn = vk.nn
+    opt = nn.Adam(gpu, lr=1e-2)
+    return nn.Sequence([
+        nn.Dense(gpu, 20, 16, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 20, seed=seed)),
+        nn.ReLU(),
+        nn.Dense(gpu, 16, 12, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 16, seed=seed + 1)),
+        nn.Sigmoid(),
+        nn.Dense(gpu, 12, 5, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 12, seed=seed + 2)),
+    ], nn.SoftmaxCrossEntropyLoss(), fuse=fuse)
+
+
+def _params(net):
+    return [np.asarray(p).copy() for L in net.L if hasattr(L, "w") for p in (L.w.value, L.b.value)]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3"])
+def test_fused_sequence_and_graph_replay_are_bit_identical(gpu, vk, prec):
+    """Dense+activation fusion and CUDA-graph replay change how many kernels
+    run, not the float32 results: parameters and losses match eager,
+    unfused steps bit for bit."""
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((32, 20)).astype(f32)
+    Y = np.eye(5, dtype=f32)[rng.integers(0, 5, 32)]
+    old = gpu.matmul_precision
+    gpu.matmul_precision = prec
+    try:
+        ref = _mlp(vk, gpu, fuse=False)
+        fused = _mlp(vk, gpu, fuse=True)
+        graphed = _mlp(vk, gpu, fuse=True)
+        x, y = vk.Array(gpu, data=X), vk.Array(gpu, data=Y)
+        losses = []
+        for _ in range(4):
+            _, l = ref.train(x, y)
+            losses.append(np.asarray(l).copy())
+        for i in range(4):
+            _, l = fused.train(x, y)
+            np.testing.assert_array_equal(np.asarray(l), losses[i])
+        graphed.train(x, y)
+        step = graphed.compile(x, y)
+        for i in range(1, 4):
+            _, l = step()
+            np.testing.assert_array_equal(np.asarray(l), losses[i])
+        for a, b, c in zip(_params(ref), _params(fused), _params(graphed)):
+            np.testing.assert_array_equal(a, b)
+            np.testing.assert_array_equal(a, c)
+    finally:
+        gpu.matmul_precision = old
+
+
+def test_graph_capture_replays_ops(gpu, vk):
+    x = vk.Array(gpu, data=np.arange(8, dtype=f32))
+    g = vk.graph.Graph(gpu)
+    with g:
+        y = (x * 2.0).exp()
+        s = y.sum()
+    g.launch()
+    np.testing.assert_allclose(np.asarray(y), np.exp(np.arange(8) * 2.0), rtol=1e-6)
+    x[:] = 1.0                     # host write, uploaded by launch(flush=...)
+    g.launch(flush=[x])
+    np.testing.assert_allclose(np.asarray(y), np.full(8, np.exp(2.0)), rtol=1e-6)
+    np.testing.assert_allclose(np.asarray(s), [8 * np.exp(2.0)], rtol=1e-6)

@@ -17,5 +17,6 @@ required; importing without it raises ImportError.
 from .vkarray import GPU, U32Array, Shape, Array, zeros
 from . import random
 from . import nn
+from . import graph
 
 __all__ = ["GPU", "U32Array", "Shape", "Array", "zeros", "random", "nn"]

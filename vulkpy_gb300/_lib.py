@@ -97,6 +97,13 @@ _SIGS = {
     "vkc_cross_entropy": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
     "vkc_adam_update": ([vp, vp, vp, vp, vp, sz, f64, f64, f64, f64, f64, f64], i32),
     "vkc_sgd_update": ([vp, vp, vp, sz, f64], i32),
+    "vkc_adam_update_dev": ([vp, vp, vp, vp, vp, sz, f64, f64, f64, f64, vp], i32),
+    "vkc_activation_backward": ([vp, i32, vp, vp, vp, sz], i32),
+    "vkc_softmax_ce_backward": ([vp, vp, vp, vp, sz, f32], i32),
+    "vkc_graph_begin": ([vp], i32),
+    "vkc_graph_end": ([vp, C.POINTER(vp)], i32),
+    "vkc_graph_launch": ([vp], i32),
+    "vkc_graph_destroy": ([vp], i32),
     "vkc_adagrad_update": ([vp, vp, vp, vp, sz, f64, f64], i32),
 }
 

@@ -136,7 +136,93 @@ k_adagrad(float* value, const float* grad, float* h, size_t n, float nlr, float 
   }
 }
 
+// Running powers for the device-resident Adam variant: p *= beta, in double
+// exactly like the Python floats of AdamState (optimizers.py:241-242).
+__global__ void k_adam_powers(double* p, double beta1, double beta2) {
+  p[0] *= beta1;
+  p[1] *= beta2;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_adam_dev(float* value, const float* grad, float* m, float* v, size_t n, float b1, float c1, float b2, float c2,
+           const double* powers, float eps, float nlr) {
+  const float d1 = (float)(1.0 - powers[0]), d2 = (float)(1.0 - powers[1]);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float g = grad[i];
+    float mi = __fadd_rn(__fmul_rn(m[i], b1), __fmul_rn(c1, g));
+    float vi = __fadd_rn(__fmul_rn(v[i], b2), __fmul_rn(c2, __fmul_rn(g, g)));
+    m[i] = mi;
+    v[i] = vi;
+    float mhat = __fdiv_rn(mi, d1);
+    float vhat = __fadd_rn(__fsqrt_rn(__fdiv_rn(vi, d2)), eps);
+    mhat = __fmul_rn(mhat, nlr);
+    mhat = __fdiv_rn(mhat, vhat);
+    value[i] = __fadd_rn(value[i], mhat);
+  }
+}
+
+// ReLU: dx = max(sign(y), 0) * dy; Sigmoid / Softmax diagonal: ((1 - y) * y) * dy.
+template <int ACT>
+__global__ void __launch_bounds__(kThreads)
+k_act_backward(const float* y, const float* dy, float* dx, size_t n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const float yi = y[i];
+    if (ACT == VKC_ACT_RELU) {
+      float s = yi > 0.f ? 1.f : (yi < 0.f ? -1.f : yi);
+      s = fmaxf(s, 0.f);
+      dx[i] = __fmul_rn(s, dy[i]);
+    } else {
+      dx[i] = __fmul_rn(__fmul_rn(__fsub_rn(1.0f, yi), yi), dy[i]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_sce_backward(const float* p, const float* y, float* dx, size_t n, float scale) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    dx[i] = __fmul_rn(__fsub_rn(p[i], y[i]), scale);
+}
+
 }  // namespace
+
+VKC_EXPORT int vkc_adam_update_dev(vkc_device_t dev, float* value, const float* grad, float* m, float* v, size_t n,
+                                   double lr, double beta1, double beta2, double eps, double* powers) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(value && grad && m && v && powers, "NULL buffer");
+  k_adam_powers<<<1, 1, 0, dev->stream>>>(powers, beta1, beta2);
+  int r = vkc::check_launch("adam_powers");
+  if (r != VKC_OK || n == 0) return r;
+  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  k_adam_dev<<<grid, kThreads, 0, dev->stream>>>(value, grad, m, v, n, (float)beta1, (float)(1.0 - beta1),
+                                                 (float)beta2, (float)(1.0 - beta2), powers, (float)eps,
+                                                 (float)(-lr));
+  return vkc::check_launch("adam_dev");
+}
+
+VKC_EXPORT int vkc_activation_backward(vkc_device_t dev, int act, const float* y, const float* dy, float* dx,
+                                       size_t n) {
+  VKC_BIND(dev);
+  if (n == 0) return VKC_OK;
+  VKC_REQUIRE(y && dy && dx, "NULL buffer");
+  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  if (act == VKC_ACT_RELU) k_act_backward<VKC_ACT_RELU><<<grid, kThreads, 0, dev->stream>>>(y, dy, dx, n);
+  else if (act == VKC_ACT_SIGMOID) k_act_backward<VKC_ACT_SIGMOID><<<grid, kThreads, 0, dev->stream>>>(y, dy, dx, n);
+  else return vkc::set_error(VKC_ERR_INVALID, "activation %d has no backward kernel", act);
+  return vkc::check_launch("activation_backward");
+}
+
+VKC_EXPORT int vkc_softmax_ce_backward(vkc_device_t dev, const float* p, const float* y, float* dx, size_t n,
+                                       float scale) {
+  VKC_BIND(dev);
+  if (n == 0) return VKC_OK;
+  VKC_REQUIRE(p && y && dx, "NULL buffer");
+  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  k_sce_backward<<<grid, kThreads, 0, dev->stream>>>(p, y, dx, n, scale);
+  return vkc::check_launch("softmax_ce_backward");
+}
 
 VKC_EXPORT int vkc_dense_forward(vkc_device_t dev, int precision, const float* x, const float* w, const float* bias,
                                  float* y, int64_t batch, int64_t in_dim, int64_t out_dim, int act) {

@@ -217,6 +217,9 @@ VKC_EXPORT int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void*
   VKC_REQUIRE(dptr && (src || bytes == 0), "NULL argument");
   *dptr = nullptr;
   if (bytes == 0) return VKC_OK;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VKC_CUDA(cudaStreamIsCapturing(dev->stream, &cap));
+  VKC_REQUIRE(cap == cudaStreamCaptureStatusNone, "host uploads are not allowed while the stream is captured");
   std::lock_guard<std::mutex> lk(dev->mu);
   // Allocate and copy on the copy stream so that the upload does not queue
   // behind compute work; the compute stream then waits for the copy.
@@ -345,5 +348,58 @@ VKC_EXPORT int vkc_job_destroy(vkc_job_t job) {
   if (!job) return VKC_OK;
   cudaEventDestroy(job->ev);
   delete job;
+  return VKC_OK;
+}
+
+// ---- CUDA graphs --------------------------------------------------------------
+
+struct vkc_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  vkc_device_t dev = nullptr;
+};
+
+VKC_EXPORT int vkc_graph_begin(vkc_device_t dev) {
+  VKC_BIND(dev);
+  VKC_CUDA(cudaStreamBeginCapture(dev->stream, cudaStreamCaptureModeThreadLocal));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_graph_end(vkc_device_t dev, vkc_graph_t* out) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(out, "graph is NULL");
+  *out = nullptr;
+  cudaGraph_t g = nullptr;
+  VKC_CUDA(cudaStreamEndCapture(dev->stream, &g));
+  cudaGraphExec_t exec = nullptr;
+  // Allocations left live by the captured work are freed and re-made (same
+  // virtual address) at the next launch instead of blocking relaunch.
+  cudaError_t e = cudaGraphInstantiateWithFlags(&exec, g, cudaGraphInstantiateFlagAutoFreeOnLaunch);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return set_error(VKC_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  }
+  auto* gr = new vkc_graph();
+  gr->graph = g;
+  gr->exec = exec;
+  gr->dev = dev;
+  *out = gr;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_graph_launch(vkc_graph_t g) {
+  VKC_REQUIRE(g, "graph is NULL");
+  VKC_BIND(g->dev);
+  VKC_CUDA(cudaGraphLaunch(g->exec, g->dev->stream));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_graph_destroy(vkc_graph_t g) {
+  if (!g) return VKC_OK;
+  VKC_BIND(g->dev);
+  cudaStreamSynchronize(g->dev->stream);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
   return VKC_OK;
 }

@@ -41,27 +41,35 @@ class Dense(Module):
         self.b = Parameter(gpu, shape=(self.output_dim,), initializer=b_init, opt=b_opt, regularizer=b_reg)
 
     def forward(self, x: Array) -> Array:
+        return self.forward_act(x, _lib.ACT_NONE)
+
+    def forward_act(self, x: Array, act: int) -> Array:
+        """y = act(x W^T + b) in one kernel (the activation in the GEMM
+        epilogue, same float32 ops as the separate ReLU / Sigmoid layer)."""
         y = Array(x._gpu, shape=(x.shape[0], self.output_dim))
         check(lib.vkc_dense_forward(x._h, _PREC[x._gpu.matmul_precision], x._dptr(), self.w.value._dptr(),
                                     self.b.value._dptr(), y._buf.ptr or 0, x.shape[0], x.shape[1],
-                                    self.output_dim, _lib.ACT_NONE))
+                                    self.output_dim, act))
         y._written()
         return y
 
-    def backward(self, dy: Array) -> Array:
+    def backward(self, dy: Array, need_dx: bool = True) -> Array:
+        """Accumulate dW and db into the parameters' gradients and return dx
+        (not computed when ``need_dx`` is False, e.g. for the first layer)."""
         x = self._x
-        dx = Array(dy._gpu, shape=(dy.shape[0], self.input_dim))
+        dx = Array(dy._gpu, shape=(dy.shape[0], self.input_dim)) if need_dx else None
         wg = self.w.grad
         bg = self.b.grad
         check(lib.vkc_dense_backward(
             dy._h, _PREC[dy._gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy._dptr(),
-            dx._buf.ptr or 0, wg._dptr() if wg is not None else None, bg._dptr() if bg is not None else None,
-            dy.shape[0], self.input_dim, self.output_dim))
+            dx._buf.ptr if dx is not None else None, wg._dptr() if wg is not None else None,
+            bg._dptr() if bg is not None else None, dy.shape[0], self.input_dim, self.output_dim))
         if wg is not None:
             wg._written()
         if bg is not None:
             bg._written()
-        dx._written()
+        if dx is not None:
+            dx._written()
         return dx
 
     def zero_grad(self):
@@ -73,21 +81,29 @@ class Dense(Module):
         self.b.update()
 
 
+def _act_backward(act: int, y: Array, dy: Array) -> Array:
+    dx = Array(dy._gpu, shape=dy.shape)
+    check(lib.vkc_activation_backward(dy._h, act, y._dptr(), dy._dptr(), dx._buf.ptr or 0, dx._size))
+    dx._written()
+    return dx
+
+
 class ReLU(Module):
-    """max(x, 0); backward dy * max(sign(y), 0) (layers.py:158-210)."""
+    """max(x, 0); backward dy * max(sign(y), 0) (layers.py:158-210), one kernel."""
+
+    act = _lib.ACT_RELU
 
     def forward(self, x: Array) -> Array:
         return x.max(0.0)
 
     def backward(self, dy: Array) -> Array:
-        dx = self._y.sign()
-        dx.max(0.0, inplace=True)
-        dx *= dy
-        return dx
+        return _act_backward(_lib.ACT_RELU, self._y, dy)
 
 
 class Sigmoid(Module):
     """1 / (1 + exp(0 - x)); backward dy * y * (1 - y) (layers.py:213-267)."""
+
+    act = _lib.ACT_SIGMOID
 
     def forward(self, x: Array) -> Array:
         y = 0.0 - x
@@ -97,10 +113,7 @@ class Sigmoid(Module):
         return y
 
     def backward(self, dy: Array) -> Array:
-        dx = 1.0 - self._y
-        dx *= self._y
-        dx *= dy
-        return dx
+        return _act_backward(_lib.ACT_SIGMOID, self._y, dy)
 
 
 class Softmax(Module):
@@ -118,7 +131,5 @@ class Softmax(Module):
         return X
 
     def backward(self, dy: Array) -> Array:
-        dx = 1.0 - self._y
-        dx *= self._y
-        dx *= dy
-        return dx
+        # the reference's diagonal-only formula, same as Sigmoid's
+        return _act_backward(_lib.ACT_SIGMOID, self._y, dy)

@@ -94,6 +94,17 @@ class SoftmaxCrossEntropyLoss(CrossEntropyLoss):
     def backward(self) -> Array:
         return cast(Array, self._sm._y) - self._y
 
+    def grad(self) -> Array:
+        """(softmax(x) - y) * scale in one kernel: the same two float32 ops
+        as backward() followed by ReduceLoss's 1/batch scaling."""
+        p = cast(Array, self._sm._y)
+        scale = 1.0 if self.scale_backward is None else self.scale_backward(p)
+        dx = Array(p._gpu, shape=p.shape)
+        check(lib.vkc_softmax_ce_backward(p._h, p._dptr(), self._y._dptr(), dx._buf.ptr or 0, dx._size,
+                                          float(scale)))
+        dx._written()
+        return dx
+
 
 class MSELoss(ReduceLoss):
     """L = sum (y - x)^2; dL/dx = 2 (x - y) (losses.py:252-320)."""

@@ -11,7 +11,9 @@ from __future__ import annotations
 import logging
 from typing import Iterable
 
-from ..vkarray import GPU, Array, zeros
+import numpy as np
+
+from ..vkarray import GPU, Array, U32Array, zeros
 from .._lib import lib, check
 from .core import Optimizer, OptimizerState
 
@@ -89,6 +91,9 @@ class AdamState(OptimizerState):
         self.v: Array = zeros(self.opt.gpu, shape=shape)
         self.beta1t: float = 1.0
         self.beta2t: float = 1.0
+        # the same running powers on the device (two doubles), advanced by the
+        # update kernel itself so that a captured training step can be replayed
+        self._powers = U32Array(self.opt.gpu, data=np.array([1.0, 1.0], dtype=np.float64).view(np.uint32))
 
     def grad2diff(self, grad: Array) -> Array:
         diff = zeros(self.opt.gpu, shape=grad.shape)
@@ -98,9 +103,10 @@ class AdamState(OptimizerState):
     def apply(self, value: Array, grad: Array):
         self.beta1t *= self.opt.beta1
         self.beta2t *= self.opt.beta2
-        check(lib.vkc_adam_update(value._h, value._dptr(), grad._dptr(), self.m._dptr(), self.v._dptr(),
-                                  value._size, float(self.opt.lr), float(self.opt.beta1), float(self.opt.beta2),
-                                  float(self.opt.eps), self.beta1t, self.beta2t))
+        check(lib.vkc_adam_update_dev(value._h, value._dptr(), grad._dptr(), self.m._dptr(), self.v._dptr(),
+                                      value._size, float(self.opt.lr), float(self.opt.beta1),
+                                      float(self.opt.beta2), float(self.opt.eps), self._powers._dptr()))
+        self._powers._written()
         self.m._written()
         self.v._written()
         value._written()

@@ -60,6 +60,7 @@ class _Device:
         self.idx = idx
         self.seq = 0        # ops issued
         self.done = 0       # ops known to be complete
+        self.capture = None  # the Graph being captured on this device, if any
         sm = C.c_int()
         name = C.create_string_buffer(256)
         check(lib.vkc_device_info(h, C.byref(sm), name, 256))
@@ -237,24 +238,43 @@ def _host_buffer(shape, dtype) -> Tuple[np.ndarray, bool]:
 
 
 class _DevBuf:
-    """Device allocation, freed stream-ordered when garbage collected."""
+    """Device allocation, freed stream-ordered when garbage collected.
 
-    __slots__ = ("dev", "ptr", "nbytes")
+    While a graph is being captured on the device, new allocations become
+    graph memory: freed inside the capture they are graph free nodes; still
+    live at the end of the capture they belong to the graph (re-made at the
+    same address on every launch, released when the graph is).  Frees of
+    older buffers during a capture are deferred until it ends."""
+
+    __slots__ = ("dev", "ptr", "nbytes", "graph")
 
     def __init__(self, dev: _Device, nbytes: int, src: Optional[np.ndarray] = None):
         self.dev = dev
         self.nbytes = nbytes
+        self.graph = dev.capture
         p = C.c_void_p()
         if src is not None and nbytes > 0:
             check(lib.vkc_upload(dev.h, src.ctypes.data, nbytes, C.byref(p)))
         else:
             check(lib.vkc_alloc(dev.h, nbytes, C.byref(p)))
         self.ptr = p.value
+        if self.graph is not None and self.ptr:
+            self.graph._allocated.add(self.ptr)
 
     def __del__(self):
         try:
-            if self.ptr:
-                lib.vkc_free(self.dev.h, self.ptr)
+            if not self.ptr:
+                return
+            cap = self.dev.capture
+            if self.graph is not None:
+                if cap is self.graph:          # freed inside its own capture
+                    self.graph._allocated.discard(self.ptr)
+                    lib.vkc_free(self.dev.h, self.ptr)
+                return                         # otherwise the graph owns it
+            if cap is not None:
+                cap._deferred.append(self.ptr)
+                return
+            lib.vkc_free(self.dev.h, self.ptr)
         except Exception:  # interpreter shutdown
             pass
 
@@ -369,13 +389,21 @@ class _GPUArray(Resource):
     def _dptr(self) -> int:
         """Device pointer for reading (uploads pending host writes first)."""
         self._ensure_device()
+        cap = self._gpu._dev.capture
+        if cap is not None:
+            cap._touch(self, write=False)
         return self._buf.ptr or 0
 
     def _written(self):
         """Record that an op on the stream (re)wrote this array."""
         self._dev_valid = True
         self._host_valid = False
-        self.job = self._gpu._dev.issued()
+        dev = self._gpu._dev
+        if dev.capture is not None:
+            dev.capture._touch(self, write=True)
+            self.job = None
+            return
+        self.job = dev.issued()
 
     # -- host access
     @property
