@@ -26,12 +26,28 @@ k_gather(const float* a, size_t n_a, const uint32_t* idx, size_t n_idx, float* c
   float4* c4 = reinterpret_cast<float4*>(c);
   bool bad = false;
   auto load = [&](uint32_t j) -> float {
-    if ((size_t)j < n_a) return a[j];
+    if ((size_t)j < n_a) return __ldg(a + j);
     bad = true;
     return __int_as_float(0x7fc00000);
   };
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nvec; i += stride) {
-    uint4 j = i4[i];
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // two index vectors per iteration: 8 independent random reads in flight
+  for (; i + stride < nvec; i += 2 * stride) {
+    const uint4 j0 = i4[i], j1 = i4[i + stride];
+    float4 v0, v1;
+    v0.x = load(j0.x);
+    v0.y = load(j0.y);
+    v0.z = load(j0.z);
+    v0.w = load(j0.w);
+    v1.x = load(j1.x);
+    v1.y = load(j1.y);
+    v1.z = load(j1.z);
+    v1.w = load(j1.w);
+    c4[i] = v0;
+    c4[i + stride] = v1;
+  }
+  for (; i < nvec; i += stride) {
+    const uint4 j = i4[i];
     float4 v;
     v.x = load(j.x);
     v.y = load(j.y);
@@ -107,7 +123,7 @@ VKC_EXPORT int vkc_gather(vkc_device_t dev, const float* a, size_t n_a, const ui
   VKC_REQUIRE(a && idx && c, "NULL buffer");
   const bool vec = ((((uintptr_t)idx) | ((uintptr_t)c)) & 15u) == 0;
   if (vec) {
-    unsigned grid = vkc::stream_grid(dev, (n_idx >> 2) + 1, kThreads);
+    unsigned grid = vkc::stream_grid(dev, (n_idx >> 3) + 1, kThreads);
     k_gather<<<grid, kThreads, 0, dev->stream>>>(a, n_a, idx, n_idx, c, dev->err_word);
   } else {
     unsigned grid = vkc::stream_grid(dev, n_idx, kThreads);

@@ -379,7 +379,20 @@ k_cols(const float* a, size_t prev, size_t axis, size_t post, int splits, float*
 #pragma unroll
   for (int w = 0; w < VW; ++w) acc[w].init();
   const float* base = a + i * axis * post + j;
-  for (size_t k = k0; k < k1; ++k) {
+  size_t k = k0;
+  if constexpr (VW == 4) {
+    // four rows per iteration: independent loads in flight, applied in order
+    for (; k + 3 < k1; k += 4) {
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = *reinterpret_cast<const float4*>(base + (k + u) * post);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        acc[0].push(v[u].x); acc[1].push(v[u].y); acc[2].push(v[u].z); acc[3].push(v[u].w);
+      }
+    }
+  }
+  for (; k < k1; ++k) {
     if constexpr (VW == 4) {
       float4 v = *reinterpret_cast<const float4*>(base + k * post);
       acc[0].push(v.x); acc[1].push(v.y); acc[2].push(v.z); acc[3].push(v.w);
@@ -494,15 +507,15 @@ VKC_EXPORT int vkc_reduce_all(vkc_device_t dev, int op, int precision, const flo
   VKC_REQUIRE(precision >= VKC_RED_PLAIN && precision <= VKC_RED_COMPENSATED, "bad precision %d", precision);
   switch (op) {
     case VKC_SUM:
-      if (precision == VKC_RED_COMPENSATED) return reduce_all_impl<VKC_SUM, true, 1>(dev, a, n, out, scale);
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_impl<VKC_SUM, true, 16>(dev, a, n, out, scale);
       if (precision == VKC_RED_PAIRWISE) return reduce_all_impl<VKC_SUM, false, 16>(dev, a, n, out, scale);
       return reduce_all_impl<VKC_SUM, false, 1>(dev, a, n, out, scale);
     case VKC_PROD:
-      if (precision == VKC_RED_COMPENSATED) return reduce_all_impl<VKC_PROD, true, 1>(dev, a, n, out, scale);
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_impl<VKC_PROD, true, 16>(dev, a, n, out, scale);
       if (precision == VKC_RED_PAIRWISE) return reduce_all_impl<VKC_PROD, false, 16>(dev, a, n, out, scale);
       return reduce_all_impl<VKC_PROD, false, 1>(dev, a, n, out, scale);
-    case VKC_MAXIMUM: return reduce_all_impl<VKC_MAXIMUM, false, 1>(dev, a, n, out, scale);
-    case VKC_MINIMUM: return reduce_all_impl<VKC_MINIMUM, false, 1>(dev, a, n, out, scale);
+    case VKC_MAXIMUM: return reduce_all_impl<VKC_MAXIMUM, false, 16>(dev, a, n, out, scale);
+    case VKC_MINIMUM: return reduce_all_impl<VKC_MINIMUM, false, 16>(dev, a, n, out, scale);
     default: return vkc::set_error(VKC_ERR_INVALID, "unknown reduce op %d", op);
   }
 }
@@ -600,15 +613,15 @@ VKC_EXPORT int vkc_reduce_all_noalloc(vkc_device_t dev, int op, int precision, c
   if (r != VKC_OK) return r;
   switch (op) {
     case VKC_SUM:
-      if (precision == VKC_RED_COMPENSATED) return reduce_all_noalloc_impl<VKC_SUM, true, 1>(dev, a, n, out, scale, partials);
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_noalloc_impl<VKC_SUM, true, 16>(dev, a, n, out, scale, partials);
       if (precision == VKC_RED_PAIRWISE) return reduce_all_noalloc_impl<VKC_SUM, false, 16>(dev, a, n, out, scale, partials);
       return reduce_all_noalloc_impl<VKC_SUM, false, 1>(dev, a, n, out, scale, partials);
     case VKC_PROD:
-      if (precision == VKC_RED_COMPENSATED) return reduce_all_noalloc_impl<VKC_PROD, true, 1>(dev, a, n, out, scale, partials);
+      if (precision == VKC_RED_COMPENSATED) return reduce_all_noalloc_impl<VKC_PROD, true, 16>(dev, a, n, out, scale, partials);
       if (precision == VKC_RED_PAIRWISE) return reduce_all_noalloc_impl<VKC_PROD, false, 16>(dev, a, n, out, scale, partials);
       return reduce_all_noalloc_impl<VKC_PROD, false, 1>(dev, a, n, out, scale, partials);
-    case VKC_MAXIMUM: return reduce_all_noalloc_impl<VKC_MAXIMUM, false, 1>(dev, a, n, out, scale, partials);
-    case VKC_MINIMUM: return reduce_all_noalloc_impl<VKC_MINIMUM, false, 1>(dev, a, n, out, scale, partials);
+    case VKC_MAXIMUM: return reduce_all_noalloc_impl<VKC_MAXIMUM, false, 16>(dev, a, n, out, scale, partials);
+    case VKC_MINIMUM: return reduce_all_noalloc_impl<VKC_MINIMUM, false, 16>(dev, a, n, out, scale, partials);
     default: return vkc::set_error(VKC_ERR_INVALID, "unknown reduce op %d", op);
   }
 }
