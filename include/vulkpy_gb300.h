@@ -303,6 +303,21 @@ int vkc_activation_backward(vkc_device_t dev, int act, const float* y, const flo
  * ReduceLoss scaling of losses.py:70-86); dx may alias p. */
 int vkc_softmax_ce_backward(vkc_device_t dev, const float* p, const float* y, float* dx, size_t n,
                             float scale);
+/* Float64 versions of vkc_dense_forward/backward, vkc_activation_backward,
+ * vkc_cross_entropy and vkc_softmax_ce_backward: the same hand-written
+ * math in double, for checking gradients against float64 finite
+ * differences.  No reference counterpart (vulkpy is float32 only). */
+int vkc_dense_forward_f64(vkc_device_t dev, const double* x, const double* w, const double* bias,
+                          double* y, int64_t batch, int64_t in_dim, int64_t out_dim, int act);
+int vkc_dense_backward_f64(vkc_device_t dev, const double* x, const double* w, const double* dy,
+                           double* dx, double* dw, double* db, int64_t batch, int64_t in_dim,
+                           int64_t out_dim);
+int vkc_activation_backward_f64(vkc_device_t dev, int act, const double* y, const double* dy,
+                                double* dx, size_t n);
+int vkc_cross_entropy_f64(vkc_device_t dev, const double* x, const double* y, double* loss_rows,
+                          double* p_out, int64_t rows, int64_t cols, int softmax);
+int vkc_softmax_ce_backward_f64(vkc_device_t dev, const double* p, const double* y, double* dx,
+                                size_t n, double scale);
 /* value += (-lr) * grad (optimizers.py:39-52). */
 int vkc_sgd_update(vkc_device_t dev, float* value, const float* grad, size_t n, double lr);
 /* h += g^2; value += (g / (sqrt(h) + eps)) * (-lr)  (optimizers.py:120-139). */

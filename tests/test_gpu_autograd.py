@@ -32,27 +32,26 @@ def problem():
     return X, Y, [W1, b1, W2, b2]
 
 
-def _torch_grads(problem, precision="fp32"):
+def _torch_grads(problem, precision="fp32", dtype=None):
     import vulkpy_gb300.autograd as A
+    dtype = dtype or torch.float32
     X, Y, params = problem
     dev = torch.device("cuda:0")
-    t = [torch.tensor(p, device=dev, requires_grad=True) for p in params]
-    x = torch.tensor(X, device=dev)
-    y = torch.tensor(Y, device=dev)
+    t = [torch.tensor(p, device=dev, dtype=dtype, requires_grad=True) for p in params]
+    x = torch.tensor(X, device=dev, dtype=dtype)
+    y = torch.tensor(Y, device=dev, dtype=dtype)
     h = A.dense(x, t[0], t[1], act="relu", precision=precision)
     z = A.dense(h, t[2], t[3], precision=precision)
     loss = A.softmax_cross_entropy(z, y)
     loss.backward()
     torch.cuda.synchronize()
-    return float(loss), [p.grad.cpu().numpy() for p in t]
+    return float(loss.detach()), [p.grad.cpu().numpy() for p in t]
 
 
-def test_gradients_match_fp64_finite_differences(problem):
+def _fd_relative_error(problem, grads):
     X, Y, params = problem
-    loss, grads = _torch_grads(problem)
     p64 = [p.astype(np.float64) for p in params]
     X64, Y64 = X.astype(np.float64), Y.astype(np.float64)
-    assert abs(loss - _loss64(p64, X64, Y64)) < 1e-5
     rng = np.random.default_rng(2)
     h = 1e-6
     ours, fd = [], []
@@ -66,8 +65,25 @@ def test_gradients_match_fp64_finite_differences(problem):
             fd.append((_loss64(plus, X64, Y64) - _loss64(minus, X64, Y64)) / (2 * h))
             ours.append(grads[k].flat[i])
     ours, fd = np.array(ours), np.array(fd)
-    rel = np.linalg.norm(ours - fd) / np.linalg.norm(fd)
+    return np.linalg.norm(ours - fd) / np.linalg.norm(fd)
+
+
+def test_fp64_kernels_match_fp64_finite_differences(problem):
+    """The hand-written kernels instantiated in float64: FD check at 1e-6."""
+    X, Y, params = problem
+    loss, grads = _torch_grads(problem, dtype=torch.float64)
+    assert abs(loss - _loss64([p.astype(np.float64) for p in params], X.astype(np.float64),
+                              Y.astype(np.float64))) < 1e-12
+    rel = _fd_relative_error(problem, grads)
     assert rel < 1e-6, rel
+
+
+def test_fp32_kernels_within_float32_rounding_of_finite_differences(problem):
+    """The float32 kernels against the same float64 FD: the difference is the
+    float32 rounding of the forward and backward sums (~4e-6 here)."""
+    _, grads = _torch_grads(problem)
+    rel = _fd_relative_error(problem, grads)
+    assert rel < 2e-5, rel
 
 
 def test_split_bf16_gradients_close_to_fp64(problem):

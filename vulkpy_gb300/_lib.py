@@ -99,6 +99,11 @@ _SIGS = {
     "vkc_sgd_update": ([vp, vp, vp, sz, f64], i32),
     "vkc_adam_update_dev": ([vp, vp, vp, vp, vp, sz, f64, f64, f64, f64, vp], i32),
     "vkc_activation_backward": ([vp, i32, vp, vp, vp, sz], i32),
+    "vkc_dense_forward_f64": ([vp, vp, vp, vp, vp, i64, i64, i64, i32], i32),
+    "vkc_dense_backward_f64": ([vp, vp, vp, vp, vp, vp, vp, i64, i64, i64], i32),
+    "vkc_activation_backward_f64": ([vp, i32, vp, vp, vp, sz], i32),
+    "vkc_cross_entropy_f64": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
+    "vkc_softmax_ce_backward_f64": ([vp, vp, vp, vp, sz, f64], i32),
     "vkc_softmax_ce_backward": ([vp, vp, vp, vp, sz, f32], i32),
     "vkc_graph_begin": ([vp], i32),
     "vkc_graph_end": ([vp, C.POINTER(vp)], i32),

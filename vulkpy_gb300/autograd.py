@@ -34,8 +34,8 @@ _PREC = {"fp32": _lib.MM_FP32, "bf16": _lib.MM_BF16, "bf16x3": _lib.MM_BF16X3}
 @contextlib.contextmanager
 def _on_torch_stream(t: torch.Tensor):
     """The device handle for t's GPU, with work routed to torch's stream."""
-    if not t.is_cuda or t.dtype != torch.float32:
-        raise TypeError("vulkpy_gb300.autograd needs float32 CUDA tensors")
+    if not t.is_cuda or t.dtype not in (torch.float32, torch.float64):
+        raise TypeError("vulkpy_gb300.autograd needs float32 (or float64, for checking) CUDA tensors")
     dev = _Device.get(t.device.index or 0, 0.0)
     check(lib.vkc_device_set_stream(dev.h, torch.cuda.current_stream(t.device).cuda_stream))
     try:
@@ -49,16 +49,19 @@ def _p(t: torch.Tensor) -> int:
 
 
 class DenseFunction(torch.autograd.Function):
-    """y = act(x W^T + b)."""
+    """y = act(x W^T + b).  float64 tensors run the float64 kernels."""
 
     @staticmethod
     def forward(ctx, x, W, b, act: int, precision: int):
         x, W, b = x.contiguous(), W.contiguous(), b.contiguous()
         B, I = x.shape
         O = W.shape[0]
-        y = torch.empty((B, O), device=x.device, dtype=torch.float32)
+        y = torch.empty((B, O), device=x.device, dtype=x.dtype)
         with _on_torch_stream(x) as h:
-            check(lib.vkc_dense_forward(h, precision, _p(x), _p(W), _p(b), _p(y), B, I, O, act))
+            if x.dtype == torch.float64:
+                check(lib.vkc_dense_forward_f64(h, _p(x), _p(W), _p(b), _p(y), B, I, O, act))
+            else:
+                check(lib.vkc_dense_forward(h, precision, _p(x), _p(W), _p(b), _p(y), B, I, O, act))
         ctx.save_for_backward(x, W, y)
         ctx.act, ctx.precision = act, precision
         return y
@@ -69,16 +72,21 @@ class DenseFunction(torch.autograd.Function):
         dy = dy.contiguous()
         B, I = x.shape
         O = W.shape[0]
+        f64 = x.dtype == torch.float64
         dW = torch.zeros_like(W)
-        db = torch.zeros((O,), device=x.device, dtype=torch.float32)
+        db = torch.zeros((O,), device=x.device, dtype=x.dtype)
         dx = torch.empty_like(x) if ctx.needs_input_grad[0] else None
         with _on_torch_stream(x) as h:
             g = dy
             if ctx.act != _lib.ACT_NONE:
                 g = torch.empty_like(dy)
-                check(lib.vkc_activation_backward(h, ctx.act, _p(y), _p(dy), _p(g), g.numel()))
-            check(lib.vkc_dense_backward(h, ctx.precision, _p(x), _p(W), _p(g), _p(dx) if dx is not None else None,
-                                         _p(dW), _p(db), B, I, O))
+                fn = lib.vkc_activation_backward_f64 if f64 else lib.vkc_activation_backward
+                check(fn(h, ctx.act, _p(y), _p(dy), _p(g), g.numel()))
+            pdx = _p(dx) if dx is not None else None
+            if f64:
+                check(lib.vkc_dense_backward_f64(h, _p(x), _p(W), _p(g), pdx, _p(dW), _p(db), B, I, O))
+            else:
+                check(lib.vkc_dense_backward(h, ctx.precision, _p(x), _p(W), _p(g), pdx, _p(dW), _p(db), B, I, O))
         return dx, dW, db, None, None
 
 
@@ -89,10 +97,11 @@ class SoftmaxCrossEntropyFunction(torch.autograd.Function):
     def forward(ctx, x, y):
         x, y = x.contiguous(), y.contiguous()
         R, Cn = x.shape
-        rows = torch.empty((R,), device=x.device, dtype=torch.float32)
+        rows = torch.empty((R,), device=x.device, dtype=x.dtype)
         p = torch.empty_like(x)
         with _on_torch_stream(x) as h:
-            check(lib.vkc_cross_entropy(h, _p(x), _p(y), _p(rows), _p(p), R, Cn, 1))
+            fn = lib.vkc_cross_entropy_f64 if x.dtype == torch.float64 else lib.vkc_cross_entropy
+            check(fn(h, _p(x), _p(y), _p(rows), _p(p), R, Cn, 1))
         ctx.save_for_backward(p, y)
         return rows.mean()
 
@@ -101,7 +110,8 @@ class SoftmaxCrossEntropyFunction(torch.autograd.Function):
         p, y = ctx.saved_tensors
         dx = torch.empty_like(p)
         with _on_torch_stream(p) as h:
-            check(lib.vkc_softmax_ce_backward(h, _p(p), _p(y), _p(dx), dx.numel(), 1.0 / p.shape[0]))
+            fn = lib.vkc_softmax_ce_backward_f64 if p.dtype == torch.float64 else lib.vkc_softmax_ce_backward
+            check(fn(h, _p(p), _p(y), _p(dx), dx.numel(), 1.0 / p.shape[0]))
         return dx * dloss, None
 
 

@@ -285,12 +285,16 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
+// With gridDim.z > 1 the K blocks are split across CTAs (blockIdx.z takes
+// blocks [z*kps, (z+1)*kps)) and each CTA writes its raw fp32 partial tile to
+// partial[z][M][N]; k_splitk_reduce then adds the partials in z order and
+// applies the epilogue, so results do not depend on scheduling.
 template <int STAGES>
 __global__ void __launch_bounds__(kThreadsTC, 1)
 k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
              const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
              int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-             uint32_t* err) {
+             uint32_t* err, float* __restrict__ partial, int kps) {
   constexpr int BN = 128;
   using Cfg = TcCfg<BN, true, STAGES>;
   constexpr uint32_t kCols = BN * kAccBufs;  // 512: all of TMEM
@@ -310,7 +314,9 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
-  const int nk = (K + kBK - 1) / kBK;
+  const int nk_all = (K + kBK - 1) / kBK;
+  const int kb0 = blockIdx.z * kps;
+  const int nk = max(0, min(nk_all, kb0 + kps) - kb0);  // K blocks of this CTA
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -348,10 +354,11 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
       const int s = kb % STAGES;
       if (*abort_flag || !mbar_wait(empty_bar(s), ((kb / STAGES) & 1) ^ 1)) { ok = false; break; }
       mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
-      tma_load_2d(stage_a(s), &map_a, full_bar(s), kb * kBK, m0);
-      tma_load_2d(stage_b(s), &map_b, full_bar(s), kb * kBK, n0);
-      tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kb * kBK, m0);
-      tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kb * kBK, n0);
+      const int kx = (kb0 + kb) * kBK;
+      tma_load_2d(stage_a(s), &map_a, full_bar(s), kx, m0);
+      tma_load_2d(stage_b(s), &map_b, full_bar(s), kx, n0);
+      tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kx, m0);
+      tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kx, n0);
       ++issued;
     }
     if (!ok) {
@@ -424,6 +431,15 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
       for (int rr = 0; rr < 32; ++rr) {
         const int grow = m0 + q * 32 + rr;
         if (grow >= M) break;
+        if (partial) {  // split K: raw partial sums, epilogue after the reduction
+          float* prow = partial + ((int64_t)blockIdx.z * M + grow) * N;
+#pragma unroll
+          for (int i = 0; i < BN / 32; ++i) {
+            const int j = i * 32 + lane;
+            if (n0 + j < N) prow[n0 + j] = tile[rr * (BN + 1) + j];
+          }
+          continue;
+        }
         float* crow = C + (int64_t)grow * ldc;
 #pragma unroll
         for (int i = 0; i < BN / 32; ++i) {
@@ -558,6 +574,26 @@ int launch_tc(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, co
   return check_launch("gemm_tc");
 }
 
+// C = act(alpha * sum_z partial[z] + beta * C + bias), z in order.
+__global__ void __launch_bounds__(256)
+k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
+                float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
+  const int64_t total = M * N;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    float s = partial[i];
+    for (int z = 1; z < splits; ++z) s += partial[(int64_t)z * total + i];
+    const int64_t r = i / N, col = i - r * N;
+    float* c = C + r * ldc + col;
+    float v = alpha * s;
+    if (beta != 0.f) v += beta * *c;
+    if (bias) v += bias[col];
+    if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+    else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+    *c = v;
+  }
+}
+
 template <int STAGES>
 int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
                  const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C,
@@ -569,10 +605,33 @@ int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb,
     VKC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
     attr_set = true;
   }
-  dim3 grid((unsigned)((N + 127) / 128), (unsigned)((M + kBM - 1) / kBM));
+  const int64_t tiles = ((N + 127) / 128) * ((M + kBM - 1) / kBM);
+  const int nk = (int)((K + kBK - 1) / kBK);
+  // Split K when the tiles alone would leave most SMs idle; at least 2 K
+  // blocks per split and no empty split.
+  int splits = 1;
+  if (tiles * 2 <= dev->sm_count && nk >= 4) {
+    splits = (int)std::min<int64_t>((dev->sm_count + tiles - 1) / tiles, nk / 2);
+    splits = std::max(1, std::min(splits, 16));
+  }
+  const int kps = (nk + splits - 1) / splits;
+  splits = (nk + kps - 1) / kps;
+  float* partial = nullptr;
+  if (splits > 1) {
+    int r = scratch_alloc(dev, sizeof(float) * (size_t)splits * M * N, (void**)&partial);
+    if (r != VKC_OK) return r;
+  }
+  dim3 grid((unsigned)((N + 127) / 128), (unsigned)((M + kBM - 1) / kBM), (unsigned)splits);
   kern<<<grid, kThreadsTC, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
-                                                      epi.bias, epi.act, dev->err_word);
-  return check_launch("gemm_tc_x3");
+                                                      epi.bias, epi.act, dev->err_word, partial, kps);
+  int r = check_launch("gemm_tc_x3");
+  if (r == VKC_OK && splits > 1) {
+    unsigned g = stream_grid(dev, (size_t)(M * N), 256);
+    k_splitk_reduce<<<g, 256, 0, dev->stream>>>(partial, splits, M, N, alpha, beta, C, ldc, epi.bias, epi.act);
+    r = check_launch("splitk_reduce");
+  }
+  scratch_free(dev, partial);
+  return r;
 }
 
 }  // namespace
