@@ -250,6 +250,8 @@ def gpu_arm(args, rank, world, dist):
     if not args.no_extra:
         extra["matmul"] = matmul_study(vk, gpu, timer)
         extra["mlp"] = mlp_study(vk, gpu, timer)
+        extra["batched"] = batched_study(vk, gpu, timer)
+        extra["chain"] = chain_study(vk, gpu, timer)
 
     result = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -432,6 +434,123 @@ def mlp_study(vk, gpu, timer, steps=50):
     res["speedup_bf16x3_graph_vs_fp32_graph"] = round(res["bf16x3_graph"]["steps_per_s"] /
                                                       res["fp32_graph"]["steps_per_s"], 2)
     return res
+
+
+def batched_study(vk, gpu, timer, n_models=64, steps=10):
+    """64 independent 2-layer MLPs of uneven sizes (seed 2: input width in
+    [17,1021], hidden in [32,2048], output in [2,64], batch in [1,512]),
+    Dense-ReLU-Dense, MSE loss, SGD(1e-2).  One step trains all 64 models.
+    Compared: the per-op eager path (fp32, one stream) and the whole step
+    captured in one CUDA graph with one parallel branch per model (fp32 SIMT
+    and split-bf16x3 tensor-core GEMMs)."""
+    nn = vk.nn
+    rng = np.random.default_rng(2)
+    dims = []
+    for _ in range(n_models):
+        i_ = int(rng.integers(17, 1022)); h_ = int(rng.integers(32, 2049))
+        o_ = int(rng.integers(2, 65)); b_ = int(rng.integers(1, 513))
+        dims.append((i_, h_, o_, b_))
+    data = [(rng.standard_normal((b, i)).astype(np.float32), rng.standard_normal((b, o)).astype(np.float32))
+            for i, h, o, b in dims]
+    flop = sum(6 * b * (i * h + h * o) for i, h, o, b in dims)
+
+    def build(seed0):
+        nets = []
+        for k, (i, h, o, b) in enumerate(dims):
+            opt = nn.SGD(lr=1e-2)
+            nets.append(nn.Sequence([
+                nn.Dense(gpu, i, h, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, i, seed=seed0 + k)),
+                nn.ReLU(),
+                nn.Dense(gpu, h, o, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, h, seed=seed0 + 1000 + k)),
+            ], nn.MSELoss()))
+        return nets
+
+    arrays = [(vk.Array(gpu, data=x), vk.Array(gpu, data=y)) for x, y in data]
+    res = {"models": n_models, "flop_per_step": flop}
+
+    def timed(fn, reps):
+        gpu.wait()
+        t0 = timer.mark()
+        for _ in range(reps):
+            fn()
+        t1 = timer.mark()
+        gpu.wait()
+        ms = timer.ms(t0, t1) / reps
+        timer.free(t0, t1)
+        return {"steps_per_s": round(1000.0 / ms, 1), "ms_per_step": round(ms, 3),
+                "tflops": round(flop / (ms * 1e-3) / 1e12, 2)}
+
+    for prec in ("fp32", "bf16x3"):
+        gpu.matmul_precision = prec
+        nets = build(7)
+        def eager():
+            for net, (x, y) in zip(nets, arrays):
+                net.train(x, y)
+        eager()
+        if prec == "fp32":
+            res["eager_fp32"] = timed(eager, steps)
+        g = vk.graph.Graph(gpu)
+        with g:
+            for net, (x, y) in zip(nets, arrays):
+                with gpu.branch():
+                    net.train(x, y)
+        g.launch()
+        res[f"graph_{prec}"] = timed(g.launch, steps * 5)
+        del g, nets
+    gpu.matmul_precision = "fp32"
+    res["speedup_graph_bf16x3_vs_eager_fp32"] = round(res["graph_bf16x3"]["steps_per_s"] /
+                                                      res["eager_fp32"]["steps_per_s"], 2)
+    return res
+
+
+def chain32(x, y):
+    """A fixed 32-op elementwise chain over two same-shape arrays."""
+    t = x * 1.0001 + y
+    t = t.tanh()
+    t = t * y - 0.5
+    t = t.exp()
+    t = t.max(0.25).min(4.0)
+    t = t.log() * 0.5
+    t = t + x * 0.125
+    t = t.sin() * t.cos()
+    t = t / (y.abs() + 1.0)
+    t = t.clamp(-2.0, 2.0)
+    t = t ** 2.0 + 1.0
+    t = t.sqrt() - x
+    t = t.atan() * 2.0
+    t = (t - y) * (t + y)
+    t = t.tanh() + t.sign()
+    return t * 0.5
+
+
+def chain_study(vk, gpu, timer, n=4096, reps=20):
+    """The 32-op chain on (4096, 4096) fp32: op by op (32 launches, every
+    intermediate written and re-read) vs one fused kernel (reads x, y once,
+    writes the result once); results must be bit-identical."""
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((n, n), dtype=np.float32)
+    Y = rng.uniform(0.5, 2.0, (n, n)).astype(np.float32)
+    x, y = vk.Array(gpu, data=X), vk.Array(gpu, data=Y)
+    fused = vk.fusion.fuse(chain32)
+    a = chain32(x, y)
+    b = fused(x, y)
+    same = bool(np.array_equal(np.asarray(a), np.asarray(b)))
+    ops = fused.source(x, y).count("const float t")
+    out = {"shape": [n, n], "ops": ops, "bit_identical": same}
+    for label, fn in (("per_op", lambda: chain32(x, y)), ("fused", lambda: fused(x, y))):
+        fn()
+        gpu.wait()
+        t0 = timer.mark()
+        for _ in range(reps):
+            r = fn()
+        t1 = timer.mark()
+        gpu.wait()
+        ms = timer.ms(t0, t1) / reps
+        timer.free(t0, t1)
+        out[label] = {"ms": round(ms, 4), "io_gbs": round(12 * n * n / (ms * 1e-3) / 1e9, 1)}
+    out["speedup"] = round(out["per_op"]["ms"] / out["fused"]["ms"], 2)
+    out["note"] = "io_gbs counts the fused kernel's 12 B/element (x, y in, result out) for both"
+    return out
 
 
 # ---------------------------------------------------------------- CPU oracle

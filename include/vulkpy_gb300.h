@@ -144,6 +144,17 @@ int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms);
 /* Number of kernels this library has launched since load (all devices). */
 int vkc_launch_count(uint64_t* count);
 
+/* ---- fused elementwise kernels (no reference counterpart: vulkpy runs one
+ * shader per op).  `source` is CUDA C defining
+ *   extern "C" __global__ void <name>(P p)
+ * with struct P { const float* in[8]; float* out[4]; unsigned long long n; };
+ * it is compiled once per device with NVRTC for this GPU (-fmad=false) and
+ * cached.  launch: in/out are 16-byte aligned device arrays of n floats. */
+typedef struct vkc_kernel* vkc_kernel_t;
+int vkc_jit_compile(vkc_device_t dev, const char* source, const char* name, vkc_kernel_t* kernel);
+int vkc_jit_launch(vkc_device_t dev, vkc_kernel_t kernel, const float* const* in, int n_in,
+                   float* const* out, int n_out, size_t n);
+
 /* ---- CUDA graphs (no reference counterpart: vulkpy submits every op as
  * its own Vulkan job, _vkarray.cc:403-438) ---------------------------------
  * begin: start capturing the device's stream; every entry point called on
@@ -152,6 +163,14 @@ int vkc_launch_count(uint64_t* count);
  * end: stop and instantiate; allocations still live at the end are re-made
  * at the same addresses on every launch.  launch: replay on the stream. */
 typedef struct vkc_graph* vkc_graph_t;
+/* Extra streams for independent work (e.g. one branch per model): create a
+ * non-blocking stream on the device, and make `waiter` wait for everything
+ * queued on `signaler` so far (an event record + wait; inside a capture this
+ * becomes a graph dependency, so fork/join patterns capture as parallel
+ * branches).  Route work to a stream with vkc_device_set_stream. */
+int vkc_stream_create(vkc_device_t dev, void** stream);
+int vkc_stream_destroy(vkc_device_t dev, void* stream);
+int vkc_stream_wait(vkc_device_t dev, void* waiter, void* signaler);
 int vkc_graph_begin(vkc_device_t dev);
 int vkc_graph_end(vkc_device_t dev, vkc_graph_t* graph);
 int vkc_graph_launch(vkc_graph_t graph);

@@ -167,3 +167,47 @@ def test_graph_capture_replays_ops(gpu, vk):
     g.launch(flush=[x])
     np.testing.assert_allclose(np.asarray(y), np.full(8, np.exp(2.0)), rtol=1e-6)
     np.testing.assert_allclose(np.asarray(s), [8 * np.exp(2.0)], rtol=1e-6)
+
+
+def test_branches_in_a_graph_match_sequential_eager(gpu, vk):
+    """Several independent models trained in parallel graph branches give the
+    same parameters as training them one after another eagerly."""
+    rng = np.random.default_rng(5)
+    shapes = [(17, 40, 3, 9), (64, 33, 8, 1), (30, 129, 5, 31)]
+    def build():
+        nets = []
+        for k, (i, h, o, b) in enumerate(shapes):
+            opt = vk.nn.SGD(lr=1e-2)
+            nets.append(vk.nn.Sequence([
+                vk.nn.Dense(gpu, i, h, w_opt=opt, b_opt=opt, w_init=vk.nn.HeNormal(gpu, i, seed=k)),
+                vk.nn.ReLU(),
+                vk.nn.Dense(gpu, h, o, w_opt=opt, b_opt=opt, w_init=vk.nn.HeNormal(gpu, h, seed=10 + k)),
+            ], vk.nn.MSELoss()))
+        return nets
+    data = [(vk.Array(gpu, data=rng.standard_normal((b, i)).astype(f32)),
+             vk.Array(gpu, data=rng.standard_normal((b, o)).astype(f32))) for i, h, o, b in shapes]
+    ref, par = build(), build()
+    for _ in range(3):
+        for net, (x, y) in zip(ref, data):
+            net.train(x, y)
+    for net, (x, y) in zip(par, data):
+        net.train(x, y)
+    g = vk.graph.Graph(gpu)
+    with g:
+        for net, (x, y) in zip(par, data):
+            with gpu.branch():
+                net.train(x, y)
+    g.launch()
+    g.launch()
+    for a, b in zip(ref, par):
+        for pa, pb in zip(_params(a), _params(b)):
+            np.testing.assert_array_equal(pa, pb)
+    # eager branches (no graph) too
+    eager = build()
+    for _ in range(3):
+        for net, (x, y) in zip(eager, data):
+            with gpu.branch():
+                net.train(x, y)
+    for a, b in zip(ref, eager):
+        for pa, pb in zip(_params(a), _params(b)):
+            np.testing.assert_array_equal(pa, pb)

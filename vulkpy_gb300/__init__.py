@@ -18,5 +18,6 @@ from .vkarray import GPU, U32Array, Shape, Array, zeros
 from . import random
 from . import nn
 from . import graph
+from . import fusion
 
 __all__ = ["GPU", "U32Array", "Shape", "Array", "zeros", "random", "nn"]

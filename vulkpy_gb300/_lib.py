@@ -105,6 +105,11 @@ _SIGS = {
     "vkc_cross_entropy_f64": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
     "vkc_softmax_ce_backward_f64": ([vp, vp, vp, vp, sz, f64], i32),
     "vkc_softmax_ce_backward": ([vp, vp, vp, vp, sz, f32], i32),
+    "vkc_jit_compile": ([vp, C.c_char_p, C.c_char_p, C.POINTER(vp)], i32),
+    "vkc_jit_launch": ([vp, vp, C.POINTER(vp), i32, C.POINTER(vp), i32, sz], i32),
+    "vkc_stream_create": ([vp, C.POINTER(vp)], i32),
+    "vkc_stream_destroy": ([vp, vp], i32),
+    "vkc_stream_wait": ([vp, vp, vp], i32),
     "vkc_graph_begin": ([vp], i32),
     "vkc_graph_end": ([vp, C.POINTER(vp)], i32),
     "vkc_graph_launch": ([vp], i32),

@@ -359,6 +359,35 @@ struct vkc_graph {
   vkc_device_t dev = nullptr;
 };
 
+VKC_EXPORT int vkc_stream_create(vkc_device_t dev, void** stream) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(stream, "stream is NULL");
+  cudaStream_t s = nullptr;
+  VKC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *stream = (void*)s;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_stream_destroy(vkc_device_t dev, void* stream) {
+  if (!stream) return VKC_OK;
+  VKC_BIND(dev);
+  VKC_CUDA(cudaStreamDestroy((cudaStream_t)stream));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_stream_wait(vkc_device_t dev, void* waiter, void* signaler) {
+  VKC_BIND(dev);
+  cudaStream_t w = waiter ? (cudaStream_t)waiter : dev->own_stream;
+  cudaStream_t s = signaler ? (cudaStream_t)signaler : dev->own_stream;
+  cudaEvent_t ev;
+  VKC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ev, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(w, ev, 0);
+  cudaEventDestroy(ev);  // released once the wait has been recorded
+  if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "stream wait: %s", cudaGetErrorString(e));
+  return VKC_OK;
+}
+
 VKC_EXPORT int vkc_graph_begin(vkc_device_t dev) {
   VKC_BIND(dev);
   VKC_CUDA(cudaStreamBeginCapture(dev->stream, cudaStreamCaptureModeThreadLocal));

@@ -61,6 +61,9 @@ class _Device:
         self.seq = 0        # ops issued
         self.done = 0       # ops known to be complete
         self.capture = None  # the Graph being captured on this device, if any
+        self.streams = [None]  # stack of current streams (None: the device's own)
+        self.spare = []        # side streams for branches
+        self.deferred = []     # (ptr, graph) frees held back while branches are open
         sm = C.c_int()
         name = C.create_string_buffer(256)
         check(lib.vkc_device_info(h, C.byref(sm), name, 256))
@@ -101,6 +104,47 @@ class _Device:
         target = self.seq
         check(lib.vkc_device_synchronize(self.h))
         self.done = max(self.done, target)
+
+    # -- freeing ------------------------------------------------------------
+    def release(self, ptr: int, graph) -> None:
+        """Free a device buffer, stream-ordered, respecting open branches and
+        graph captures (see _DevBuf)."""
+        if graph is not None and self.capture is not graph:
+            return                                  # owned by its graph
+        if len(self.streams) > 1:                   # a branch is open
+            self.deferred.append((ptr, graph))
+            return
+        cap = self.capture
+        if cap is not None and graph is not cap:    # older buffer: after the capture
+            cap._deferred.append(ptr)
+            return
+        if graph is not None:
+            graph._allocated.discard(ptr)
+        lib.vkc_free(self.h, ptr)
+
+    # -- branches -----------------------------------------------------------
+    def branch_enter(self):
+        parent = self.streams[-1]
+        if self.spare:
+            s = self.spare.pop()
+        else:
+            p = C.c_void_p()
+            check(lib.vkc_stream_create(self.h, C.byref(p)))
+            s = p.value
+        check(lib.vkc_stream_wait(self.h, s, parent))      # fork
+        check(lib.vkc_device_set_stream(self.h, s))
+        self.streams.append(s)
+
+    def branch_exit(self):
+        s = self.streams.pop()
+        parent = self.streams[-1]
+        check(lib.vkc_device_set_stream(self.h, parent))
+        check(lib.vkc_stream_wait(self.h, parent, s))      # join
+        self.spare.append(s)
+        if len(self.streams) == 1:
+            pending, self.deferred = self.deferred, []
+            for ptr, graph in pending:
+                self.release(ptr, graph)
 
 
 class Job:
@@ -161,6 +205,25 @@ class GPU:
     def wait(self):
         """Wait for all GPU operations (GPU.wait, _vkarray.cc:560-562)."""
         self._dev.synchronize()
+
+    def branch(self):
+        """Context manager: ops inside run on a side stream that forks from the
+        current stream at entry and joins it at exit, so independent branches
+        (e.g. one per model) run concurrently; inside a graph capture they
+        become parallel branches of the graph.  Buffers released while a
+        branch is open are freed after the join."""
+        gpu = self
+
+        class _Branch:
+            def __enter__(self):
+                gpu._dev.branch_enter()
+                return self
+
+            def __exit__(self, *exc):
+                gpu._dev.branch_exit()
+                return False
+
+        return _Branch()
 
     def check_errors(self) -> int:
         """Read and clear the device error word (bit0: gather index out of range)."""
@@ -263,18 +326,8 @@ class _DevBuf:
 
     def __del__(self):
         try:
-            if not self.ptr:
-                return
-            cap = self.dev.capture
-            if self.graph is not None:
-                if cap is self.graph:          # freed inside its own capture
-                    self.graph._allocated.discard(self.ptr)
-                    lib.vkc_free(self.dev.h, self.ptr)
-                return                         # otherwise the graph owns it
-            if cap is not None:
-                cap._deferred.append(self.ptr)
-                return
-            lib.vkc_free(self.dev.h, self.ptr)
+            if self.ptr:
+                self.dev.release(self.ptr, self.graph)
         except Exception:  # interpreter shutdown
             pass
 
