@@ -252,6 +252,7 @@ def gpu_arm(args, rank, world, dist):
         extra["mlp"] = mlp_study(vk, gpu, timer)
         extra["batched"] = batched_study(vk, gpu, timer)
         extra["chain"] = chain_study(vk, gpu, timer)
+        extra["reduction_precision"] = reduction_precision_study(vk, gpu, timer)
 
     result = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -500,6 +501,43 @@ def batched_study(vk, gpu, timer, n_models=64, steps=10):
     gpu.matmul_precision = "fp32"
     res["speedup_graph_bf16x3_vs_eager_fp32"] = round(res["graph_bf16x3"]["steps_per_s"] /
                                                       res["eager_fp32"]["steps_per_s"], 2)
+    return res
+
+
+def reduction_precision_study(vk, gpu, timer, n=1 << 28):
+    """sum of 2^28 float32 values 1e6*N(0,1) + U[0,1) (generated on the GPU
+    by Xoshiro128pp seed 0), in the three summation modes, against a float64
+    sum of the same float32 values; plus the time of each mode."""
+    from vulkpy_gb300 import _lib
+    import ctypes
+    r = vk.random.Xoshiro128pp(gpu, size=1 << 20, seed=0)
+    z = r.normal(shape=(n,), mean=0.0, stddev=1e6)
+    u = r.random(shape=(n,))
+    x = z + u
+    del z, u
+    host = np.asarray(x)
+    truth = float(np.sum(host, dtype=np.float64))
+    scale = float(np.sum(np.abs(host), dtype=np.float64))
+    out = vk.Array(gpu, shape=(1,))
+    res = {"n": n, "truth_fp64": truth, "sum_abs": scale}
+    for name, mode in (("plain", _lib.RED_PLAIN), ("pairwise", _lib.RED_PAIRWISE),
+                       ("compensated", _lib.RED_COMPENSATED)):
+        def run():
+            check = _lib.check
+            check(_lib.lib.vkc_reduce_all(gpu.handle, _lib.SUM, mode, x._dptr(), n, out._buf.ptr, ctypes.c_float(1.0)))
+        run()
+        gpu.wait()
+        t0 = timer.mark()
+        for _ in range(5):
+            run()
+        t1 = timer.mark()
+        gpu.wait()
+        ms = timer.ms(t0, t1) / 5
+        timer.free(t0, t1)
+        out._written()
+        v = float(np.asarray(out)[0])
+        res[name] = {"value": v, "abs_err": abs(v - truth), "err_rel_sum_abs": abs(v - truth) / scale,
+                     "gbs": round(4 * n / (ms * 1e-3) / 1e9, 1)}
     return res
 
 

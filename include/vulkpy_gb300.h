@@ -244,6 +244,15 @@ int vkc_gemm(vkc_device_t dev, int precision, int trans_a, int trans_b,
              const float* a, int64_t lda, const float* b, int64_t ldb,
              float beta, float* c, int64_t ldc);
 
+/* Split-K tuning table of the tensor-core GEMM, keyed by precision and the
+ * log2 size buckets of (m, n, k); splits = 0 removes an entry.  The table
+ * written by vulkpy_gb300/autotune.py is loaded at import; shapes without an
+ * entry use an occupancy heuristic.  get: the split count a shape will use.
+ * No reference counterpart (matmul.comp has no tiling). */
+int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k, int splits);
+int vkc_gemm_tune_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits);
+int vkc_gemm_tune_clear(void);
+
 /* ---- gather ------------------------------------------------------ */
 /* c[i] = a[idx[i]], i < n_idx.  An index >= n_a writes NaN and sets bit0 of
  * the device error word.  vkarray.py:1476-1500, gather.comp:21-26. */

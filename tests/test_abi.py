@@ -45,3 +45,19 @@ def test_null_device_is_rejected_without_gpu():
     st = _lib.lib.vkc_binary(None, _lib.ADD, None, None, None, 4)
     assert st == _lib.ERR_INVALID
     assert "NULL" in _lib.last_error()
+
+
+def test_gemm_tuning_table_host_side(tmp_path):
+    """The split-K table is host state: set/clear validate without a GPU, and a
+    table file round-trips through the loader."""
+    import json
+    from vulkpy_gb300 import _lib, autotune
+    assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 256, 1024, 784, 65) == _lib.ERR_INVALID
+    assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 256, 1024, 784, 4) == _lib.OK
+    assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 256, 1024, 784, 0) == _lib.OK   # erase
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps({"bf16x3": [[8, 10, 10, 2], [7, 12, 14, 8]]}))
+    assert autotune.load_table(str(p)) == 2
+    assert _lib.lib.vkc_gemm_tune_clear() == _lib.OK
+    autotune.load_table()   # restore the shipped table
+    assert autotune.bucket(1) == 0 and autotune.bucket(784) == 10 and autotune.bucket(1024) == 10

@@ -78,3 +78,37 @@ def test_dense_layer_on_tensor_cores(gpu, vk):
     assert rel_fro(dx, dy.astype(np.float64) @ W.astype(np.float64)) < 1e-5
     assert rel_fro(dW, dy.astype(np.float64).T @ x64) < 1e-5
     assert gpu.check_errors() == 0
+
+
+@pytest.mark.parametrize("m,n,k", [(256, 1024, 784), (64, 300, 2000), (1, 37, 4096)])
+def test_split_k_counts_agree(gpu, vk, m, n, k):
+    """Every split count the tuner may choose gives the bf16x3 accuracy, the
+    table's choice is the one used, and a fixed choice is bit-reproducible."""
+    import ctypes as C
+    from vulkpy_gb300 import _lib
+    rng = np.random.default_rng(m + n + k)
+    A = rng.standard_normal((m, k)).astype(np.float32)
+    B = rng.standard_normal((n, k)).astype(np.float32)
+    a, b = vk.Array(gpu, data=A), vk.Array(gpu, data=B)
+    exp = A.astype(np.float64) @ B.T.astype(np.float64)
+    try:
+        for s in (1, 2, 3, 8, 16):
+            assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, s) == 0
+            got = C.c_int()
+            assert _lib.lib.vkc_gemm_tune_get(gpu.handle, _lib.MM_BF16X3, m, n, k, C.byref(got)) == 0
+            assert got.value == min(s, (k + 63) // 64)
+            outs = []
+            for _ in range(2):
+                c = vk.Array(gpu, shape=(m, n))
+                st = _lib.lib.vkc_gemm(gpu.handle, _lib.MM_BF16X3, 0, 1, m, n, k, C.c_float(1.0), a._dptr(), k,
+                                       b._dptr(), k, C.c_float(0.0), c._dptr(), n)
+                assert st == 0, _lib.last_error()
+                c._written()
+                outs.append(np.asarray(c).copy())
+            assert np.array_equal(outs[0], outs[1]), s
+            assert rel_fro(outs[0], exp) < 1e-5, s
+    finally:
+        _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, 0)
+        from vulkpy_gb300 import autotune
+        autotune.load_table()
+    assert gpu.check_errors() == 0

@@ -19,5 +19,8 @@ from . import random
 from . import nn
 from . import graph
 from . import fusion
+from . import autotune as _autotune
+
+_autotune.load_table()
 
 __all__ = ["GPU", "U32Array", "Shape", "Array", "zeros", "random", "nn"]

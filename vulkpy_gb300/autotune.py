@@ -1,0 +1,141 @@
+"""
+Split-K autotuner for the split-bf16x3 tensor-core GEMM.
+
+For each size bucket (ceil(log2) of M, N and K) the tuner times every
+candidate split count on a representative problem of that bucket and keeps
+the fastest.  The result is written to ``tuning.json`` next to this file and
+loaded into the library at import (vkc_gemm_tune_set), so the choice at run
+time is a table lookup: deterministic, the same in eager runs and graph
+captures.  Buckets without an entry fall back to an occupancy heuristic.
+
+Run on the GPU:  python -m vulkpy_gb300.autotune [--quick]
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import sys
+import time
+from typing import Dict, Iterable, List, Tuple
+
+import numpy as np
+
+from . import _lib
+from ._lib import lib, check
+
+TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+CANDIDATES = (1, 2, 3, 4, 6, 8, 12, 16)
+
+
+def bucket(x: int) -> int:
+    b = 0
+    while (1 << b) < x:
+        b += 1
+    return b
+
+
+def load_table(path: str = TABLE_PATH) -> int:
+    """Load the tuning table into the library; returns the entry count."""
+    if not os.path.exists(path):
+        return 0
+    with open(path) as f:
+        data = json.load(f)
+    n = 0
+    for m, nn, k, splits in data.get("bf16x3", []):
+        # representative sizes: the top of each bucket
+        check(lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 1 << m, 1 << nn, 1 << k, int(splits)))
+        n += 1
+    return n
+
+
+def default_shapes() -> List[Tuple[int, int, int]]:
+    """Shapes of the MLP workloads (batch 256, 784-1024-1024-10 forward and
+    backward), the batched uneven MLPs, and square / skinny sizes."""
+    shapes = set()
+    for (i, o) in ((784, 1024), (1024, 1024), (1024, 10)):
+        for b in (256,):
+            shapes.add((b, o, i))      # forward  x W^T
+            shapes.add((o, i, b))      # dW = dy^T x
+            shapes.add((b, i, o))      # dx = dy W
+    rng = np.random.default_rng(2)
+    for _ in range(64):
+        i_ = int(rng.integers(17, 1022)); h_ = int(rng.integers(32, 2049))
+        o_ = int(rng.integers(2, 65)); b_ = int(rng.integers(1, 513))
+        for s in ((b_, h_, i_), (b_, o_, h_), (h_, i_, b_), (o_, h_, b_), (b_, h_, o_)):
+            shapes.add(s)
+    for s in (256, 512, 1024, 2048, 4096):
+        shapes.add((s, s, s))
+        shapes.add((128, s, 4 * s))
+    # one representative per bucket
+    rep: Dict[Tuple[int, int, int], Tuple[int, int, int]] = {}
+    for (m, n, k) in sorted(shapes):
+        rep.setdefault((bucket(m), bucket(n), bucket(k)), (m, n, k))
+    return sorted(rep.values())
+
+
+def _time_gemm(gpu, a, b, c, m, n, k, reps=5) -> float:
+    lib_ = lib
+    h = gpu.handle
+
+    def run():
+        check(lib_.vkc_gemm(h, _lib.MM_BF16X3, 0, 1, m, n, k, C.c_float(1.0), a, k, b, k, C.c_float(0.0), c, n))
+
+    run()
+    check(lib_.vkc_device_synchronize(h))
+    times = []
+    for _ in range(reps):
+        t0, t1 = C.c_void_p(), C.c_void_p()
+        check(lib_.vkc_timer_record(h, C.byref(t0)))
+        run()
+        check(lib_.vkc_timer_record(h, C.byref(t1)))
+        ms = C.c_float()
+        check(lib_.vkc_job_elapsed_ms(t0, t1, C.byref(ms)))
+        lib_.vkc_job_destroy(t0)
+        lib_.vkc_job_destroy(t1)
+        times.append(ms.value)
+    return float(np.median(times))
+
+
+def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) -> dict:
+    import vulkpy_gb300 as vk
+    gpu = vk.GPU()
+    shapes = list(shapes or default_shapes())
+    check(lib.vkc_gemm_tune_clear())
+    entries = []
+    for (m, n, k) in shapes:
+        rng = np.random.default_rng(m * 31 + n * 7 + k)
+        A = vk.Array(gpu, data=rng.standard_normal((m, k)).astype(np.float32))
+        B = vk.Array(gpu, data=rng.standard_normal((n, k)).astype(np.float32))
+        Cm = vk.Array(gpu, shape=(m, n))
+        nk = (k + 63) // 64
+        best, best_ms = 1, float("inf")
+        results = {}
+        for s in CANDIDATES:
+            if s > max(1, nk):
+                continue
+            check(lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, s))
+            ms = _time_gemm(gpu, A._dptr(), B._dptr(), Cm._buf.ptr, m, n, k)
+            results[s] = round(ms * 1e3, 1)
+            if ms < best_ms:
+                best, best_ms = s, ms
+        check(lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, best))
+        entries.append([bucket(m), bucket(n), bucket(k), best])
+        if verbose:
+            print(f"M={m} N={n} K={k}: best splits {best} ({best_ms * 1e3:.1f} us)  {results}", flush=True)
+    table = {"bf16x3": entries, "device": vk.GPU()._dev.name,
+             "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
+             "candidates": list(CANDIDATES)}
+    return table
+
+
+def main():
+    table = tune(default_shapes()[:12] if "--quick" in sys.argv else None)
+    out = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else TABLE_PATH
+    with open(out, "w") as f:
+        json.dump(table, f, indent=1)
+    print(f"wrote {len(table['bf16x3'])} entries to {out}")
+
+
+if __name__ == "__main__":
+    main()

@@ -21,6 +21,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 
 namespace vkc {
@@ -574,6 +575,39 @@ int launch_tc(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, co
   return check_launch("gemm_tc");
 }
 
+// ---- split-K tuning table: (precision, log2 buckets of M, N, K) -> splits.
+// Filled from the autotuner's table at import (vkc_gemm_tune_set); shapes
+// without an entry use the occupancy heuristic below.
+std::mutex g_tune_mu;
+std::map<uint64_t, int> g_tune;
+
+inline int bucket(int64_t x) {
+  int b = 0;
+  while ((int64_t(1) << b) < x) ++b;
+  return b;
+}
+inline uint64_t tune_key(int precision, int mb, int nb, int kb) {
+  return ((uint64_t)precision << 24) | ((uint64_t)mb << 16) | ((uint64_t)nb << 8) | (uint64_t)kb;
+}
+
+int heuristic_splits(vkc_device_t dev, int64_t tiles, int nk) {
+  int splits = 1;
+  if (tiles * 2 <= dev->sm_count && nk >= 4) {
+    splits = (int)std::min<int64_t>((dev->sm_count + tiles - 1) / tiles, nk / 2);
+    splits = std::max(1, std::min(splits, 16));
+  }
+  return splits;
+}
+
+int choose_splits(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_t K, int64_t tiles, int nk) {
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(precision, bucket(M), bucket(N), bucket(K)));
+    if (it != g_tune.end()) return std::max(1, std::min(it->second, std::max(1, nk)));
+  }
+  return heuristic_splits(dev, tiles, nk);
+}
+
 // C = act(alpha * sum_z partial[z] + beta * C + bias), z in order.
 __global__ void __launch_bounds__(256)
 k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
@@ -607,13 +641,9 @@ int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb,
   }
   const int64_t tiles = ((N + 127) / 128) * ((M + kBM - 1) / kBM);
   const int nk = (int)((K + kBK - 1) / kBK);
-  // Split K when the tiles alone would leave most SMs idle; at least 2 K
-  // blocks per split and no empty split.
-  int splits = 1;
-  if (tiles * 2 <= dev->sm_count && nk >= 4) {
-    splits = (int)std::min<int64_t>((dev->sm_count + tiles - 1) / tiles, nk / 2);
-    splits = std::max(1, std::min(splits, 16));
-  }
+  // Split K when the tiles alone would leave most SMs idle (tuning table
+  // first, then the occupancy heuristic); no empty split.
+  int splits = choose_splits(dev, VKC_MM_BF16X3, M, N, K, tiles, nk);
   const int kps = (nk + splits - 1) / splits;
   splits = (nk + kps - 1) / kps;
   float* partial = nullptr;
@@ -635,6 +665,33 @@ int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb,
 }
 
 }  // namespace
+
+}  // namespace vkc
+
+VKC_EXPORT int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k, int splits) {
+  VKC_REQUIRE(splits >= 0 && splits <= 64, "splits out of range");
+  std::lock_guard<std::mutex> lk(vkc::g_tune_mu);
+  auto key = vkc::tune_key(precision, vkc::bucket(m), vkc::bucket(n), vkc::bucket(k));
+  if (splits == 0) vkc::g_tune.erase(key);
+  else vkc::g_tune[key] = splits;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_gemm_tune_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits) {
+  VKC_REQUIRE(dev && splits, "NULL argument");
+  const int64_t tiles = ((n + 127) / 128) * ((m + 127) / 128);
+  const int nk = (int)((k + 63) / 64);
+  *splits = vkc::choose_splits(dev, precision, m, n, k, tiles, nk);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_gemm_tune_clear(void) {
+  std::lock_guard<std::mutex> lk(vkc::g_tune_mu);
+  vkc::g_tune.clear();
+  return VKC_OK;
+}
+
+namespace vkc {
 
 int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
             const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
