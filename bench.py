@@ -253,6 +253,7 @@ def gpu_arm(args, rank, world, dist):
         extra["batched"] = batched_study(vk, gpu, timer)
         extra["chain"] = chain_study(vk, gpu, timer)
         extra["reduction_precision"] = reduction_precision_study(vk, gpu, timer)
+        extra["train_loop"] = train_loop_study(vk, gpu)
 
     result = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -559,6 +560,96 @@ def chain32(x, y):
     t = (t - y) * (t + y)
     t = t.tanh() + t.sign()
     return t * 0.5
+
+
+def train_loop_study(vk, gpu, epochs=100, batch=32):
+    """The classification example's loop (4-128-128-3, ReLU, Softmax,
+    CrossEntropyLoss(sum), Adam lr 1e-4, batch 32, 100 epochs, 120/30 split)
+    on a synthetic Iris-shaped set (3 Gaussian classes of 50 rows in 4-D,
+    numpy seed 0).  Each epoch reads back the train loss and the test-set
+    class predictions, as the example prints them.  Three loops:
+      host:   numpy shuffle, one upload per batch, numpy argmax (the
+              example's own structure);
+      device: data resident, device permutation + row gathers, device argmax;
+      graph:  the device epoch captured once and replayed."""
+    import time as _time
+    nn = vk.nn
+    rng = np.random.default_rng(0)
+    means = rng.uniform(1.0, 7.0, size=(3, 4))
+    x = np.concatenate([rng.normal(means[c], 0.45, size=(50, 4)) for c in range(3)]).astype(np.float32)
+    lab = np.repeat(np.arange(3), 50)
+    order = rng.permutation(150)
+    x, lab = x[order], lab[order]
+    y = np.identity(3, dtype=np.float32)[lab]
+    tx, ty, vx, vlab = x[:120], y[:120], x[120:], lab[120:]
+
+    def make():
+        opt = nn.Adam(gpu, lr=1e-4)
+        return nn.Sequence([
+            nn.Dense(gpu, 4, 128, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 4, seed=1)), nn.ReLU(),
+            nn.Dense(gpu, 128, 128, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 128, seed=2)), nn.ReLU(),
+            nn.Dense(gpu, 128, 3, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, 128, seed=3)), nn.Softmax(),
+        ], nn.CrossEntropyLoss(reduce="sum"))
+
+    res = {"epochs": epochs, "batch": batch, "rows": 120, "data": "synthetic Iris-shaped (numpy seed 0)"}
+    VX = vk.Array(gpu, data=vx)
+
+    # host loop
+    net = make()
+    hrng = np.random.default_rng(1)
+    idx = np.arange(120)
+    gpu.wait()
+    t0 = _time.perf_counter()
+    for _ in range(epochs):
+        hrng.shuffle(idx)
+        total = vk.Array(gpu, shape=(1,))
+        total[:] = 0
+        for s in range(0, 120, batch):
+            b = idx[s:s + batch]
+            _, loss = net.train(vk.Array(gpu, data=tx[b]), vk.Array(gpu, data=ty[b]))
+            total += loss
+        pred = np.argmax(np.asarray(net.predict(VX)), axis=1)
+        float(np.asarray(total)[0])
+    dt = _time.perf_counter() - t0
+    res["host"] = {"epochs_per_s": round(epochs / dt, 1), "accuracy": float(np.mean(pred == vlab))}
+
+    X, Y = vk.Array(gpu, data=tx), vk.Array(gpu, data=ty)
+
+    def epoch(net, r):
+        total = vk.zeros(gpu, shape=(1,))
+        for xb, yb in nn.minibatches(X, Y, batch, rng=r):
+            _, loss = net.train(xb, yb)
+            total += loss
+        return total, net.predict(VX).argmax(axis=1)
+
+    net, r = make(), vk.random.Xoshiro128pp(gpu, seed=1)
+    epoch(net, r)   # builds the row-range tables
+    gpu.wait()
+    t0 = _time.perf_counter()
+    for _ in range(epochs):
+        total, cls = epoch(net, r)
+        float(np.asarray(total)[0])
+        pred = np.asarray(cls)
+    dt = _time.perf_counter() - t0
+    res["device"] = {"epochs_per_s": round(epochs / dt, 1), "accuracy": float(np.mean(pred == vlab))}
+
+    net, r = make(), vk.random.Xoshiro128pp(gpu, seed=1)
+    epoch(net, r)
+    g = vk.graph.Graph(gpu)
+    with g:
+        total, cls = epoch(net, r)
+    g.launch()
+    gpu.wait()
+    t0 = _time.perf_counter()
+    for _ in range(epochs):
+        g.launch()
+        float(np.asarray(total)[0])
+        pred = np.asarray(cls)
+    dt = _time.perf_counter() - t0
+    res["graph"] = {"epochs_per_s": round(epochs / dt, 1), "accuracy": float(np.mean(pred == vlab))}
+    res["speedup_graph_vs_host"] = round(res["graph"]["epochs_per_s"] / res["host"]["epochs_per_s"], 2)
+    del g
+    return res
 
 
 def chain_study(vk, gpu, timer, n=4096, reps=20):

@@ -54,6 +54,9 @@ enum vkc_unary_op {
 /* reductions: vulkpy/shader/{sum,prod,maximum,minimum}{,_v1.3,_axis,_axis_rebroadcast}.comp */
 enum vkc_reduce_op { VKC_SUM = 0, VKC_PROD = 1, VKC_MAXIMUM = 2, VKC_MINIMUM = 3 };
 
+/* index reductions (numpy argmax/argmin; listed as missing in README.md:73) */
+enum vkc_arg_op { VKC_ARGMAX = 0, VKC_ARGMIN = 1 };
+
 /* summation precision for VKC_SUM / VKC_PROD over axis=None */
 enum vkc_reduce_precision {
   VKC_RED_PLAIN = 0,        /* per-thread sequential fp32, tree combine          */
@@ -262,6 +265,22 @@ int vkc_gather(vkc_device_t dev, const float* a, size_t n_a, const uint32_t* idx
  * vkarray.py:1501-1521, gather_axis.comp:24-43, U32Array.to_onehot 239-253. */
 int vkc_gather_axis(vkc_device_t dev, const float* a, size_t prev, size_t axis, size_t post,
                     const uint32_t* idx, size_t n_idx, float* c);
+
+/* ---- index reductions and permutations (no reference kernel) ---- */
+/* The reference names argmax/argmin as missing (README.md:73) and its
+ * training example computes them with numpy on the host
+ * (example/02-nn.py:96).  numpy semantics: the first index of the extreme
+ * value, the first NaN if any, -0.0 == +0.0.  out[0] = index; n < 2^32. */
+int vkc_arg_reduce_all(vkc_device_t dev, int op, const float* a, size_t n, uint32_t* out);
+/* out[p, q] = arg-extreme over k of a[p, k, q], k < axis < 2^32. */
+int vkc_arg_reduce_axis(vkc_device_t dev, int op, const float* a, size_t prev, size_t axis, size_t post,
+                        uint32_t* out);
+/* out[0..n) = a pseudo-random permutation of 0..n-1, keyed by four uint32
+ * drawn from the state stream (as vkc_xoshiro_u32 with n = 4): a 6-round
+ * Feistel network on the smallest even-bit domain >= n, cycle-walked into
+ * [0, n).  Replaces the host shuffle of example/02-nn.py:82 ("TODO:
+ * Implement GPU shuffle()"); README.md:77 lists shuffle as missing. */
+int vkc_xoshiro_permutation(vkc_device_t dev, uint32_t* state, uint32_t size, uint32_t* out, size_t n);
 
 /* ---- xoshiro128++ PRNG ---------------------------------------- */
 /* Fill state[4*size] (device) exactly like PRNG::Xoshiro128pp's constructor

@@ -76,6 +76,7 @@ def lib():
             "matmul": ([vp, vp, vp, i64, i64, i64], None),
             "gather": ([vp, u64, vp, u64, vp], None),
             "gather_axis": ([vp, u64, u64, u64, vp, u64, vp], None),
+            "permutation": ([vp, vp, u64], None),
             "oracle_threads": ([], i32),
         }
         for name, (args, res) in sig.items():

@@ -62,6 +62,15 @@ class Xoshiro128pp:
         lib().randrange(_p(u), _p(out), int(n), int(low), int(high) - 1)
         return out
 
+    def permutation(self, n: int) -> np.ndarray:
+        """Four keys from the u32 stream, then the keyed Feistel permutation
+        (vkoracle.c ``permutation``)."""
+        out = np.empty(int(n), dtype=np.uint32)
+        if n:   # an empty permutation draws nothing
+            key = self.u32(4)
+            lib().permutation(_p(key), _p(out), int(n))
+        return out
+
 
 # ------------------------------------------------------------ elementwise
 def binary(op: int, a, b) -> np.ndarray:

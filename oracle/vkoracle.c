@@ -297,6 +297,45 @@ EXPORT void gather_axis(const float* a, uint64_t prev, uint64_t axis, uint64_t p
   }
 }
 
+/* ------------------------------------------------------------- permutation
+ * No reference kernel (the reference shuffles on the host,
+ * example/02-nn.py:82).  Restates the library's keyed Feistel permutation:
+ * 6 rounds of murmur3's fmix32 on R ^ key[r % 4] ^ r * 0x9E3779B9 over d/2-bit
+ * halves, d = max(2, ceil(log2 n)) rounded up to even, cycle-walked into
+ * [0, n). */
+static inline uint32_t fmix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x85EBCA6Bu;
+  x ^= x >> 13;
+  x *= 0xC2B2AE35u;
+  x ^= x >> 16;
+  return x;
+}
+
+EXPORT void permutation(const uint32_t* key, uint32_t* out, uint64_t n) {
+  int d = 0;
+  while (d < 64 && ((uint64_t)1 << d) < n) ++d;
+  if (d < 2) d = 2;
+  if (d & 1) ++d;
+  const int h = d / 2;
+  const uint32_t mask = h >= 32 ? 0xFFFFFFFFu : ((1u << h) - 1u);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    uint64_t x = (uint64_t)i;
+    do {
+      uint32_t l = (uint32_t)(x >> h), r = (uint32_t)x & mask;
+      for (uint32_t k = 0; k < 6; ++k) {
+        uint32_t f = fmix32(r ^ key[k & 3] ^ (k * 0x9E3779B9u)) & mask;
+        uint32_t nl = r;
+        r = l ^ f;
+        l = nl;
+      }
+      x = ((uint64_t)l << h) | r;
+    } while (x >= n);
+    out[i] = (uint32_t)x;
+  }
+}
+
 EXPORT int oracle_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -101,3 +101,37 @@ def test_c_abi_direct_calls(gpu):
     done = C.c_int()
     assert lib.vkc_job_query(j, C.byref(done)) == 0 and done.value == 1
     assert lib.vkc_job_destroy(j) == 0
+
+
+def test_graph_collected_during_another_capture(gpu, vk):
+    """A launched graph that the garbage collector destroys while another
+    graph is being captured must not invalidate that capture; it is
+    destroyed (and its memory freed) once the capture ends."""
+    import gc
+    x = vk.Array(gpu, data=np.arange(4096, dtype=np.float32))
+    gc.collect()
+    gc.disable()
+    try:
+        old = vk.graph.Graph(gpu)
+        with old:
+            y = (x + 1.0) * 2.0
+        old.launch()
+        np.testing.assert_array_equal(np.asarray(y), (np.arange(4096, dtype=np.float32) + 1.0) * 2.0)
+        cycle = {"g": old, "y": y}
+        cycle["self"] = cycle
+        del old, y, cycle
+        g = vk.graph.Graph(gpu)
+        with g:
+            z = x * 3.0
+            gc.collect()                      # destroys `old` mid-capture
+            assert len(gpu._dev.zombies) == 1
+            with gpu.branch():
+                w = x - 1.0
+            z = z + w
+        assert gpu._dev.zombies == []
+    finally:
+        gc.enable()
+    g.launch()
+    np.testing.assert_array_equal(np.asarray(z), np.arange(4096, dtype=np.float32) * 4.0 - 1.0)
+    g.launch()
+    np.testing.assert_array_equal(np.asarray(z), np.arange(4096, dtype=np.float32) * 4.0 - 1.0)

@@ -101,3 +101,27 @@ def test_randrange_bounds():
     r = O.Xoshiro128pp(seed=4, size=16)
     v = r.randrange(10000, 10, 1000)
     assert v.min() >= 10 and v.max() < 1000
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 4, 5, 17, 1000, 65536, 65537, 1 << 20])
+def test_oracle_permutation_is_a_permutation(n):
+    from oracle.ops import Xoshiro128pp
+    p = Xoshiro128pp(7, 64).permutation(n)
+    assert p.dtype == np.uint32 and p.shape == (n,)
+    assert np.array_equal(np.sort(p), np.arange(n, dtype=np.uint32))
+    # reproducible for a seed, different for another
+    assert np.array_equal(p, Xoshiro128pp(7, 64).permutation(n))
+    if n > 16:
+        assert not np.array_equal(p, Xoshiro128pp(8, 64).permutation(n))
+        assert not np.array_equal(p, np.arange(n))
+
+
+def test_oracle_permutation_draws_four_keys():
+    from oracle.ops import Xoshiro128pp
+    a, b = Xoshiro128pp(3, 2), Xoshiro128pp(3, 2)
+    a.permutation(10)
+    b.u32(4)
+    assert np.array_equal(a.state, b.state)
+    c = Xoshiro128pp(3, 2)
+    c.permutation(0)            # draws nothing
+    assert np.array_equal(c.state, Xoshiro128pp(3, 2).state)

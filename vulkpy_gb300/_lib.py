@@ -29,6 +29,7 @@ UNARY = {name: i for i, name in enumerate(
     ["abs", "sign", "sin", "cos", "tan", "asin", "acos", "atan", "sinh", "cosh", "tanh",
      "asinh", "acosh", "atanh", "exp", "log", "exp2", "log2", "sqrt", "invsqrt", "copy"])}
 SUM, PROD, MAXIMUM, MINIMUM = range(4)
+ARGMAX, ARGMIN = range(2)
 RED_PLAIN, RED_PAIRWISE, RED_COMPENSATED = range(3)
 MM_FP32, MM_BF16, MM_BF16X3 = range(3)
 ACT_NONE, ACT_RELU, ACT_SIGMOID = range(3)
@@ -88,6 +89,9 @@ _SIGS = {
     "vkc_gemm_tune_clear": ([], i32),
     "vkc_gather": ([vp, vp, sz, vp, sz, vp], i32),
     "vkc_gather_axis": ([vp, vp, sz, sz, sz, vp, sz, vp], i32),
+    "vkc_arg_reduce_all": ([vp, i32, vp, sz, vp], i32),
+    "vkc_arg_reduce_axis": ([vp, i32, vp, sz, sz, sz, vp], i32),
+    "vkc_xoshiro_permutation": ([vp, vp, u32, vp, sz], i32),
     "vkc_xoshiro_seed": ([vp, u64, u32, vp], i32),
     "vkc_xoshiro_u32": ([vp, vp, u32, vp, sz], i32),
     "vkc_xoshiro_f32": ([vp, vp, u32, vp, sz], i32),

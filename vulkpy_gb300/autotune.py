@@ -8,7 +8,8 @@ loaded into the library at import (vkc_gemm_tune_set), so the choice at run
 time is a table lookup: deterministic, the same in eager runs and graph
 captures.  Buckets without an entry fall back to an occupancy heuristic.
 
-Run on the GPU:  python -m vulkpy_gb300.autotune [--quick]
+Run on the GPU:
+    python -c "import vulkpy_gb300.autotune as t; t.main()" [--quick] [--out FILE]
 """
 from __future__ import annotations
 
@@ -74,7 +75,10 @@ def default_shapes() -> List[Tuple[int, int, int]]:
     return sorted(rep.values())
 
 
-def _time_gemm(gpu, a, b, c, m, n, k, reps=5) -> float:
+def _time_gemm(gpu, a, b, c, m, n, k, reps=5, calls=16) -> float:
+    """Device time of one call in ms.  The calls are captured in a CUDA
+    graph and replayed, so host-side launch cost (which a graph removes)
+    does not decide the choice."""
     lib_ = lib
     h = gpu.handle
 
@@ -83,17 +87,30 @@ def _time_gemm(gpu, a, b, c, m, n, k, reps=5) -> float:
 
     run()
     check(lib_.vkc_device_synchronize(h))
-    times = []
-    for _ in range(reps):
-        t0, t1 = C.c_void_p(), C.c_void_p()
-        check(lib_.vkc_timer_record(h, C.byref(t0)))
-        run()
-        check(lib_.vkc_timer_record(h, C.byref(t1)))
-        ms = C.c_float()
-        check(lib_.vkc_job_elapsed_ms(t0, t1, C.byref(ms)))
-        lib_.vkc_job_destroy(t0)
-        lib_.vkc_job_destroy(t1)
-        times.append(ms.value)
+    check(lib_.vkc_graph_begin(h))
+    try:
+        for _ in range(calls):
+            run()
+    finally:
+        g = C.c_void_p()
+        st = lib_.vkc_graph_end(h, C.byref(g))
+    check(st)
+    try:
+        check(lib_.vkc_graph_launch(g))
+        times = []
+        for _ in range(reps):
+            t0, t1 = C.c_void_p(), C.c_void_p()
+            check(lib_.vkc_timer_record(h, C.byref(t0)))
+            check(lib_.vkc_graph_launch(g))
+            check(lib_.vkc_timer_record(h, C.byref(t1)))
+            ms = C.c_float()
+            check(lib_.vkc_job_elapsed_ms(t0, t1, C.byref(ms)))
+            lib_.vkc_job_destroy(t0)
+            lib_.vkc_job_destroy(t1)
+            times.append(ms.value / calls)
+    finally:
+        check(lib_.vkc_device_synchronize(h))
+        lib_.vkc_graph_destroy(g)
     return float(np.median(times))
 
 

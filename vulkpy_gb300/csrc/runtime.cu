@@ -426,6 +426,11 @@ VKC_EXPORT int vkc_graph_launch(vkc_graph_t g) {
 VKC_EXPORT int vkc_graph_destroy(vkc_graph_t g) {
   if (!g) return VKC_OK;
   VKC_BIND(g->dev);
+  // The synchronisation below would invalidate a capture in progress on the
+  // stream; refuse instead (the caller destroys the graph after the capture).
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  VKC_CUDA(cudaStreamIsCapturing(g->dev->stream, &cs));
+  VKC_REQUIRE(cs == cudaStreamCaptureStatusNone, "cannot destroy a graph while a capture is active on its stream");
   cudaStreamSynchronize(g->dev->stream);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);

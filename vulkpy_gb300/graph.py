@@ -60,6 +60,7 @@ class Graph:
         for p in self._deferred:
             lib.vkc_free(self._dev.h, p)
         self._deferred = []
+        self._dev.reap()
         if exc_type is not None:
             if h.value:
                 lib.vkc_graph_destroy(h)
@@ -84,15 +85,18 @@ class Graph:
                 a.job = self._dev.issued()
 
     def __del__(self):
+        # The garbage collector may run this in the middle of another
+        # graph's capture (graphs sit in reference cycles with their arrays),
+        # where destroying a graph or freeing its memory would invalidate that
+        # capture: the device defers both until no capture or branch is open.
         try:
-            if self._h is not None:
-                lib.vkc_graph_destroy(self._h)
-                self._h = None
             # graph allocations exist once the graph has run; the last
-            # launch's live ones are released here
-            if self._launched:
-                for p in self._allocated:
-                    lib.vkc_free(self._dev.h, p)
+            # launch's live ones are released with it
+            ptrs = list(self._allocated) if self._launched else []
             self._allocated = set()
+            h, self._h = self._h, None
+            if h is not None or ptrs:
+                self._dev.zombies.append((h, ptrs))
+                self._dev.reap()
         except Exception:  # interpreter shutdown
             pass

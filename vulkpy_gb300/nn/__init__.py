@@ -17,3 +17,4 @@ from .losses import CrossEntropyLoss, SoftmaxCrossEntropyLoss, MSELoss, HuberLos
 from .regularizers import Lasso, Ridge, Elastic
 from .models import Sequence
 from .parameters import Parameter
+from .data import minibatches

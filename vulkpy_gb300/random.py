@@ -139,3 +139,32 @@ class Xoshiro128pp(PRNG):
         buf._written()
         self._state._written()
         return buf
+
+    def permutation(self, n: int) -> vk.U32Array:
+        """A pseudo-random permutation of ``0..n-1`` computed on the device.
+
+        The reference shuffles on the host (example/02-nn.py:82).  Four
+        uint32 are drawn from this generator as keys of a Feistel-network
+        bijection, so a seeded generator gives a reproducible order; each
+        index is computed independently (one launch, no sort)."""
+        n = int(n)
+        if n < 0 or n >= self._2p32:
+            raise ValueError(f"n must be in [0, 2^32), got {n}")
+        buf = vk.U32Array(self._gpu, shape=(n,))
+        check(lib.vkc_xoshiro_permutation(self._gpu._dev.h, self._state._buf.ptr, self.size,
+                                          buf._buf.ptr or 0, n))
+        buf._written()
+        if n:
+            self._state._written()
+        return buf
+
+    def shuffle(self, x: vk.Array) -> None:
+        """Shuffle ``x`` in place along its first axis (numpy
+        ``Generator.shuffle`` semantics) with ``permutation(len(x))``."""
+        if len(x.shape) == 0 or x.shape[0] <= 1:
+            return
+        y = x.gather(self.permutation(x.shape[0]), axis=0)
+        src = y._dptr()
+        x._ensure_device_for_overwrite()
+        check(lib.vkc_copy(self._gpu._dev.h, x._buf.ptr, src, x._size * 4))
+        x._written()

@@ -64,6 +64,7 @@ class _Device:
         self.streams = [None]  # stack of current streams (None: the device's own)
         self.spare = []        # side streams for branches
         self.deferred = []     # (ptr, graph) frees held back while branches are open
+        self.zombies = []      # (graph handle, its allocations) dropped during a capture
         sm = C.c_int()
         name = C.create_string_buffer(256)
         check(lib.vkc_device_info(h, C.byref(sm), name, 256))
@@ -122,6 +123,18 @@ class _Device:
             graph._allocated.discard(ptr)
         lib.vkc_free(self.h, ptr)
 
+    def reap(self) -> None:
+        """Destroy graphs (and free their memory) that were dropped while a
+        capture or a branch was open; a no-op until neither is."""
+        if self.capture is not None or len(self.streams) > 1:
+            return
+        while self.zombies:
+            h, ptrs = self.zombies.pop()
+            if h is not None:
+                lib.vkc_graph_destroy(h)
+            for p in ptrs:
+                lib.vkc_free(self.h, p)
+
     # -- branches -----------------------------------------------------------
     def branch_enter(self):
         parent = self.streams[-1]
@@ -145,6 +158,7 @@ class _Device:
             pending, self.deferred = self.deferred, []
             for ptr, graph in pending:
                 self.release(ptr, graph)
+            self.reap()
 
 
 class Job:
@@ -823,6 +837,39 @@ class Array(_GPUArray):
     def minimum(self, axis=None, keepdims: bool = False, rebroadcast: bool = False) -> "Array":
         """Minimum (vkarray.py:1368-1396)."""
         return self._reduce(_lib.MINIMUM, axis, keepdims, rebroadcast)
+
+    def _arg(self, op: int, axis, keepdims: bool) -> U32Array:
+        if self._size == 0:
+            raise ValueError("attempt to get argmax/argmin of an empty sequence")
+        if axis is None:
+            ret = U32Array(self._gpu, shape=(1,))
+            check(lib.vkc_arg_reduce_all(self._h, op, self._dptr(), self._size, ret._buf.ptr or 0))
+            ret._written()
+            if keepdims:
+                ret.reshape((1,) * len(self.shape))
+            return ret
+        if not isinstance(axis, (int, np.integer)):
+            raise ValueError("`axis` must be `int` or `None`")
+        a = _normalize_axes(axis, len(self.shape))[0]
+        shape = list(self.shape)
+        new_shape = shape[:a] + ([1] if keepdims else []) + shape[a + 1:]
+        ret = U32Array(self._gpu, shape=tuple(new_shape))
+        if ret._size:
+            check(lib.vkc_arg_reduce_axis(self._h, op, self._dptr(), _prod(shape[:a]), int(shape[a]),
+                                          _prod(shape[a + 1:]), ret._buf.ptr or 0))
+            ret._written()
+        return ret
+
+    def argmax(self, axis=None, keepdims: bool = False) -> U32Array:
+        """Index of the maximum (numpy ``argmax``: first occurrence, NaN
+        wins).  ``axis=None`` gives shape ``(1,)`` like the other full
+        reductions.  Not in the reference (README.md:73 lists it as
+        missing; example/02-nn.py:96 uses numpy on the host)."""
+        return self._arg(_lib.ARGMAX, axis, keepdims)
+
+    def argmin(self, axis=None, keepdims: bool = False) -> U32Array:
+        """Index of the minimum (numpy ``argmin`` semantics)."""
+        return self._arg(_lib.ARGMIN, axis, keepdims)
 
     def mean(self, axis=None, keepdims: bool = False, rebroadcast: bool = False) -> "Array":
         """Mean (vkarray.py:1398-1432): the sum scaled in the same launch by
