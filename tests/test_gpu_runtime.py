@@ -135,3 +135,24 @@ def test_graph_collected_during_another_capture(gpu, vk):
     np.testing.assert_array_equal(np.asarray(z), np.arange(4096, dtype=np.float32) * 4.0 - 1.0)
     g.launch()
     np.testing.assert_array_equal(np.asarray(z), np.arange(4096, dtype=np.float32) * 4.0 - 1.0)
+
+
+def test_graph_output_tracked_when_python_reuses_ids(gpu, vk):
+    """An array written by the captured ops may get the id() of a temporary
+    freed earlier in the capture; every launch must still invalidate its
+    host copy (otherwise reads after the second launch are stale)."""
+    base = np.arange(1024, dtype=np.float32)
+    x = vk.Array(gpu, data=base)
+    g = vk.graph.Graph(gpu)
+    ids = set()
+    with g:
+        for _ in range(20):
+            t = x * 2.0
+            ids.add(id(t))
+            del t
+        out = x + 1.0
+    reused = id(out) in ids
+    for k in range(4):
+        x[:] = base * (k + 1)
+        g.launch(flush=[x])
+        np.testing.assert_array_equal(np.asarray(out), base * (k + 1) + 1.0, err_msg=f"launch {k}, reused={reused}")

@@ -197,13 +197,18 @@ int launch_bcast(vkc_device_t dev, const Geom& g, const float* a, const float* b
     bool vec = (inner % 4 == 0) && aligned;
     int64_t chunk = vec ? 4 * kThreads * 4 : kThreads * 8;
     int64_t cpr = (inner + chunk - 1) / chunk;
-    unsigned grid = (unsigned)std::min<int64_t>(rows * cpr, (int64_t)dev->sm_count * 8);
-    if (vec)
+    // one unit (chunk) per block at a time: the grid is the units, capped at
+    // one wave of resident blocks
+    const size_t units = (size_t)(rows * cpr);
+    if (vec) {
+      unsigned grid = vkc::wave_grid(dev, k_bcast_rows<NIN, true, Op>, units * kThreads, kThreads);
       k_bcast_rows<NIN, true><<<grid, kThreads, 0, dev->stream>>>(g, a, b, c, out, rows, inner, chunk, cpr, op);
-    else
+    } else {
+      unsigned grid = vkc::wave_grid(dev, k_bcast_rows<NIN, false, Op>, units * kThreads, kThreads);
       k_bcast_rows<NIN, false><<<grid, kThreads, 0, dev->stream>>>(g, a, b, c, out, rows, inner, chunk, cpr, op);
+    }
   } else {
-    unsigned grid = vkc::stream_grid(dev, (size_t)total, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_bcast_elem<NIN, Op>, (size_t)total, kThreads);
     k_bcast_elem<NIN><<<grid, kThreads, 0, dev->stream>>>(g, a, b, c, out, total, op);
   }
   return vkc::check_launch("broadcast");

@@ -60,6 +60,23 @@ inline unsigned stream_grid(const vkc_device* dev, size_t work_items, int thread
   return (unsigned)(want < cap ? want : cap);
 }
 
+// Blocks of `kernel` resident per SM at `threads` threads and `smem` bytes of
+// dynamic shared memory (cudaOccupancyMaxActiveBlocksPerMultiprocessor,
+// cached per kernel; at least 1).
+int resident_blocks(const void* kernel, int threads, size_t smem = 0);
+
+// Grid for a grid-stride kernel: at most one full wave of resident blocks.
+// A grid sized for more blocks than fit (e.g. 8 per SM for a kernel whose
+// registers allow 5) runs a partial second wave that leaves SMs idle at the
+// end of the launch.
+template <class K>
+inline unsigned wave_grid(const vkc_device* dev, K* kernel, size_t work_items, int threads, size_t smem = 0) {
+  size_t want = (work_items + threads - 1) / threads;
+  if (want < 1) want = 1;
+  const size_t cap = (size_t)dev->sm_count * (size_t)resident_blocks((const void*)kernel, threads, smem);
+  return (unsigned)(want < cap ? want : cap);
+}
+
 // Stream-ordered scratch allocation on the device's current stream.
 int scratch_alloc(vkc_device_t dev, size_t bytes, void** p);
 void scratch_free(vkc_device_t dev, void* p);

@@ -99,10 +99,10 @@ int launch_map(vkc_device_t dev, const float* a, const float* b, const float* c,
   bool vec = aligned16(a) && aligned16(out) && (NIN < 2 || aligned16(b)) && (NIN < 3 || aligned16(c));
   if (vec) {
     size_t items = (n >> 2) / 2 + 1;
-    unsigned grid = vkc::stream_grid(dev, items, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_map<NIN, Op>, items, kThreads);
     k_map<NIN><<<grid, kThreads, 0, dev->stream>>>(a, b, c, out, n, op);
   } else {
-    unsigned grid = vkc::stream_grid(dev, n, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_map_scalar<NIN, Op>, n, kThreads);
     k_map_scalar<NIN><<<grid, kThreads, 0, dev->stream>>>(a, b, c, out, n, op);
   }
   return vkc::check_launch(what);
@@ -133,10 +133,10 @@ template <class T>
 int launch_fill(vkc_device_t dev, T* p, size_t n, T v) {
   if (n == 0) return VKC_OK;
   if (aligned16(p)) {
-    unsigned grid = vkc::stream_grid(dev, (n >> 2) + 1, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_fill4<T>, (n >> 2) + 1, kThreads);
     k_fill4<T><<<grid, kThreads, 0, dev->stream>>>(p, n, v);
   } else {
-    unsigned grid = vkc::stream_grid(dev, n, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_fill<T>, n, kThreads);
     k_fill<T><<<grid, kThreads, 0, dev->stream>>>(p, n, v);
   }
   return vkc::check_launch("fill");

@@ -123,10 +123,10 @@ VKC_EXPORT int vkc_gather(vkc_device_t dev, const float* a, size_t n_a, const ui
   VKC_REQUIRE(a && idx && c, "NULL buffer");
   const bool vec = ((((uintptr_t)idx) | ((uintptr_t)c)) & 15u) == 0;
   if (vec) {
-    unsigned grid = vkc::stream_grid(dev, (n_idx >> 3) + 1, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_gather, (n_idx >> 3) + 1, kThreads);
     k_gather<<<grid, kThreads, 0, dev->stream>>>(a, n_a, idx, n_idx, c, dev->err_word);
   } else {
-    unsigned grid = vkc::stream_grid(dev, n_idx, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_gather_scalar, n_idx, kThreads);
     k_gather_scalar<<<grid, kThreads, 0, dev->stream>>>(a, n_a, idx, n_idx, c, dev->err_word);
   }
   return vkc::check_launch("gather");

@@ -195,7 +195,7 @@ VKC_EXPORT int vkc_adam_update_dev(vkc_device_t dev, float* value, const float* 
   k_adam_powers<<<1, 1, 0, dev->stream>>>(powers, beta1, beta2);
   int r = vkc::check_launch("adam_powers");
   if (r != VKC_OK || n == 0) return r;
-  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  unsigned grid = vkc::wave_grid(dev, k_adam_dev, n, kThreads);
   k_adam_dev<<<grid, kThreads, 0, dev->stream>>>(value, grad, m, v, n, (float)beta1, (float)(1.0 - beta1),
                                                  (float)beta2, (float)(1.0 - beta2), powers, (float)eps,
                                                  (float)(-lr));
@@ -219,7 +219,7 @@ VKC_EXPORT int vkc_softmax_ce_backward(vkc_device_t dev, const float* p, const f
   VKC_BIND(dev);
   if (n == 0) return VKC_OK;
   VKC_REQUIRE(p && y && dx, "NULL buffer");
-  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  unsigned grid = vkc::wave_grid(dev, k_sce_backward, n, kThreads);
   k_sce_backward<<<grid, kThreads, 0, dev->stream>>>(p, y, dx, n, scale);
   return vkc::check_launch("softmax_ce_backward");
 }
@@ -295,7 +295,7 @@ VKC_EXPORT int vkc_adam_update(vkc_device_t dev, float* value, const float* grad
   const float b1 = (float)beta1, b2 = (float)beta2;
   const float c1 = (float)(1.0 - beta1), c2 = (float)(1.0 - beta2);
   const float d1 = (float)(1.0 - beta1t), d2 = (float)(1.0 - beta2t);
-  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  unsigned grid = vkc::wave_grid(dev, k_adam, n, kThreads);
   k_adam<<<grid, kThreads, 0, dev->stream>>>(value, grad, m, v, n, b1, c1, b2, c2, d1, d2, (float)eps, (float)(-lr));
   return vkc::check_launch("adam");
 }
@@ -304,7 +304,7 @@ VKC_EXPORT int vkc_sgd_update(vkc_device_t dev, float* value, const float* grad,
   VKC_BIND(dev);
   if (n == 0) return VKC_OK;
   VKC_REQUIRE(value && grad, "NULL buffer");
-  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  unsigned grid = vkc::wave_grid(dev, k_sgd, n, kThreads);
   k_sgd<<<grid, kThreads, 0, dev->stream>>>(value, grad, n, (float)(-lr));
   return vkc::check_launch("sgd");
 }
@@ -314,7 +314,7 @@ VKC_EXPORT int vkc_adagrad_update(vkc_device_t dev, float* value, const float* g
   VKC_BIND(dev);
   if (n == 0) return VKC_OK;
   VKC_REQUIRE(value && grad && h, "NULL buffer");
-  unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  unsigned grid = vkc::wave_grid(dev, k_adagrad, n, kThreads);
   k_adagrad<<<grid, kThreads, 0, dev->stream>>>(value, grad, h, n, (float)(-lr), (float)eps);
   return vkc::check_launch("adagrad");
 }

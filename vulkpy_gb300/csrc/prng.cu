@@ -299,7 +299,7 @@ VKC_EXPORT int vkc_box_muller(vkc_device_t dev, const float* u, float* out, size
   VKC_BIND(dev);
   if (n == 0) return VKC_OK;
   VKC_REQUIRE(u && out, "NULL buffer");
-  unsigned grid = vkc::stream_grid(dev, (n + 1) / 2, kThreads);
+  unsigned grid = vkc::wave_grid(dev, k_box_muller, (n + 1) / 2, kThreads);
   k_box_muller<<<grid, kThreads, 0, dev->stream>>>(u, out, n, mean, stddev);
   return vkc::check_launch("box_muller");
 }
@@ -328,7 +328,7 @@ VKC_EXPORT int vkc_xoshiro_normal(vkc_device_t dev, uint32_t* state, uint32_t si
   }
   int r = generate<kOutF32>(dev, state, size, u, m, 0, 0);
   if (r == VKC_OK) {
-    unsigned grid = vkc::stream_grid(dev, m / 2, kThreads);
+    unsigned grid = vkc::wave_grid(dev, k_box_muller, m / 2, kThreads);
     k_box_muller<<<grid, kThreads, 0, dev->stream>>>(u, out, n, mean, stddev);
     r = vkc::check_launch("box_muller");
   }

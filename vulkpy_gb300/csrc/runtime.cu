@@ -8,6 +8,7 @@
 #include <chrono>
 #include <thread>
 #include <cstring>
+#include <unordered_map>
 
 namespace vkc {
 
@@ -51,6 +52,39 @@ int scratch_alloc(vkc_device_t dev, size_t bytes, void** p) {
 
 void scratch_free(vkc_device_t dev, void* p) {
   if (p) cudaFreeAsync(p, dev->stream);
+}
+
+namespace {
+struct OccKey {
+  const void* kernel;
+  int threads;
+  size_t smem;
+  bool operator==(const OccKey& o) const { return kernel == o.kernel && threads == o.threads && smem == o.smem; }
+};
+struct OccHash {
+  size_t operator()(const OccKey& k) const {
+    return std::hash<const void*>()(k.kernel) ^ (std::hash<size_t>()(k.smem) * 31u) ^ ((size_t)k.threads << 20);
+  }
+};
+std::mutex g_occ_mu;
+std::unordered_map<OccKey, int, OccHash> g_occ;
+}  // namespace
+
+int resident_blocks(const void* kernel, int threads, size_t smem) {
+  const OccKey key{kernel, threads, smem};
+  {
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    auto it = g_occ.find(key);
+    if (it != g_occ.end()) return it->second;
+  }
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 1;
+  }
+  std::lock_guard<std::mutex> lk(g_occ_mu);
+  g_occ[key] = n;
+  return n;
 }
 
 }  // namespace vkc

@@ -40,7 +40,11 @@ class Graph:
         if arr._buf is not None and arr._buf.graph is not self:
             self._keep.setdefault(key, arr)
         if write:
-            self._written.setdefault(key, weakref.ref(arr))
+            # ids of arrays freed during the capture are reused by later
+            # objects: replace an entry that no longer names this array
+            r = self._written.get(key)
+            if r is None or r() is not arr:
+                self._written[key] = weakref.ref(arr)
             if arr._buf is not None and arr._buf.graph is self:
                 arr._graph = self   # keep the graph alive while this array lives
 
