@@ -442,9 +442,11 @@ def batched_study(vk, gpu, timer, n_models=64, steps=10):
     """64 independent 2-layer MLPs of uneven sizes (seed 2: input width in
     [17,1021], hidden in [32,2048], output in [2,64], batch in [1,512]),
     Dense-ReLU-Dense, MSE loss, SGD(1e-2).  One step trains all 64 models.
-    Compared: the per-op eager path (fp32, one stream) and the whole step
-    captured in one CUDA graph with one parallel branch per model (fp32 SIMT
-    and split-bf16x3 tensor-core GEMMs)."""
+    Compared: the per-op eager path (fp32, one stream), the whole step
+    captured in one CUDA graph with one parallel branch per model, and the
+    grouped step (nn.GroupedSequence: one persistent grouped GEMM per layer
+    and direction for all 64 models, grouped loss / bias-gradient / SGD
+    kernels), eager and captured; fp32 SIMT and split-bf16x3 tensor cores."""
     nn = vk.nn
     rng = np.random.default_rng(2)
     dims = []
@@ -499,9 +501,24 @@ def batched_study(vk, gpu, timer, n_models=64, steps=10):
         g.launch()
         res[f"graph_{prec}"] = timed(g.launch, steps * 5)
         del g, nets
+        # grouped: one launch per layer and direction for all 64 models
+        nets = build(7)
+        grp = nn.GroupedSequence(nets)
+        xs = [x for x, _ in arrays]
+        ys = [y for _, y in arrays]
+        grp.train(xs, ys)
+        res[f"grouped_eager_{prec}"] = timed(lambda: grp.train(xs, ys), steps)
+        g = vk.graph.Graph(gpu)
+        with g:
+            grp.train(xs, ys)
+        g.launch()
+        res[f"grouped_graph_{prec}"] = timed(g.launch, steps * 5)
+        del g, grp, nets
     gpu.matmul_precision = "fp32"
     res["speedup_graph_bf16x3_vs_eager_fp32"] = round(res["graph_bf16x3"]["steps_per_s"] /
                                                       res["eager_fp32"]["steps_per_s"], 2)
+    res["speedup_grouped_graph_bf16x3_vs_eager_fp32"] = round(res["grouped_graph_bf16x3"]["steps_per_s"] /
+                                                              res["eager_fp32"]["steps_per_s"], 2)
     return res
 
 

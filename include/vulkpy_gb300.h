@@ -256,6 +256,49 @@ int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k, int splits
 int vkc_gemm_tune_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits);
 int vkc_gemm_tune_clear(void);
 
+/* ---- grouped (batched, uneven) GEMM and MLP-step pieces --------- */
+/* No counterpart in the reference, which runs every Dense layer of every
+ * model as its own job (nn/layers.py:94-141, batch_affine.comp:25-39,
+ * _vkarray.cc:403-438).  One problem of a grouped call:
+ *   C = act(alpha * op(A) op(B) + beta * C + bias), then, when relu_mask is
+ *   not NULL, C *= max(sign(relu_mask), 0) elementwise (relu_mask has C's
+ *   layout: the ReLU backward of layers.py:176-181 fused into the GEMM). */
+typedef struct vkc_gemm_problem {
+  int32_t ta, tb;           /* op(A) = A^T when ta, op(B) = B^T when tb */
+  int64_t m, n, k;
+  float alpha, beta;
+  const float* a;
+  int64_t lda;
+  const float* b;
+  int64_t ldb;
+  float* c;
+  int64_t ldc;
+  const float* bias;        /* per column of C, may be NULL */
+  int32_t act;              /* vkc_activation, applied before relu_mask */
+  const float* relu_mask;   /* may be NULL */
+} vkc_gemm_problem;
+/* All `count` problems in persistent launches (128 problems per launch):
+ * the output tiles of every problem form one work list, longest K first.
+ * fp32: bit-identical to vkc_gemm per problem.  bf16x3: bit-identical to
+ * vkc_gemm when that call does not split K; bf16: accumulated per 64-wide K
+ * block in fp32 (at least as accurate as vkc_gemm's bf16). */
+int vkc_gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_problem* problems, int count);
+/* db[i][o] += sum_b dy[i][b, o] for every item (the bias gradient of
+ * layers.py:125-128), b in order, one launch per 128 items; with
+ * `overwrite` db[i][o] = the sum (equal to accumulating into a zeroed db). */
+int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
+                       const int64_t* cols, int count, int overwrite);
+/* value[i] += (-lr) * grad[i] for every tensor (optimizers.py:24-60). */
+int vkc_sgd_update_grouped(vkc_device_t dev, float* const* value, const float* const* grad, const int64_t* n,
+                           double lr, int count);
+/* MSELoss with reduce="mean" for many models (losses.py:252-320 with
+ * ReduceLoss 40-92): dx[i] = ((x - y) * 2) * float32(1/batch) (when dx is
+ * not NULL) and loss[i] = mean over rows of sum over columns of (y - x)^2
+ * (when loss is not NULL, at most 256 models; summation order differs from
+ * the per-op path, the value agrees to rounding). */
+int vkc_mse_grouped(vkc_device_t dev, const float* const* x, const float* const* y, float* const* dx,
+                    const int64_t* batch, const int64_t* cols, float* loss, int count);
+
 /* ---- gather ------------------------------------------------------ */
 /* c[i] = a[idx[i]], i < n_idx.  An index >= n_a writes NaN and sets bit0 of
  * the device error word.  vkarray.py:1476-1500, gather.comp:21-26. */

@@ -1,0 +1,221 @@
+"""Grouped GEMM and the grouped MLP training step.
+
+* fp32 grouped products equal vkc_gemm's bit for bit (same tile code);
+* split-bf16x3 grouped products equal vkc_gemm's bit for bit when that call
+  does not split K (forced through the tuning table), and stay within the
+  split method's 1e-5 relative error of float64;
+* GroupedSequence.train leaves every model's parameters exactly where its
+  own Sequence.train would, eagerly and replayed from a CUDA graph."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle.ops import rel_fro
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def vk():
+    import vulkpy_gb300
+    return vulkpy_gb300
+
+
+def _problems(rng, count):
+    shapes = [(1, 1, 1), (1, 300, 7), (129, 257, 100), (17, 5, 1021), (300, 2, 64), (256, 1024, 784),
+              (3, 2048, 33), (512, 64, 2048), (65, 129, 0), (0, 12, 9)]
+    while len(shapes) < count:
+        shapes.append((int(rng.integers(1, 513)), int(rng.integers(2, 2049)), int(rng.integers(1, 1100))))
+    return shapes[:count]
+
+
+def _run_grouped(vk, gpu, lib_, prec, specs):
+    probs = []
+    outs = []
+    for (ta, tb, M, N, K, alpha, beta, A, B, C0, bias, act, mask) in specs:
+        probs.append(lib_.GemmProblem(
+            ta=ta, tb=tb, m=M, n=N, k=K, alpha=alpha, beta=beta, a=A._dptr() if K else None,
+            lda=(M if ta else K), b=B._dptr() if K else None, ldb=(K if tb else N), c=C0._dptr(), ldc=N,
+            bias=bias._dptr() if bias is not None else None, act=act,
+            relu_mask=mask._dptr() if mask is not None else None))
+        outs.append(C0)
+    arr = (lib_.GemmProblem * len(probs))(*probs)
+    st = lib_.lib.vkc_gemm_grouped(gpu.handle, prec, arr, len(probs))
+    assert st == 0, lib_.last_error()
+    for c in outs:
+        c._written()
+    return [np.asarray(c).copy() for c in outs]
+
+
+def _specs(vk, gpu, rng, count, with_epilogue):
+    specs, host = [], []
+    for i, (M, N, K) in enumerate(_problems(rng, count)):
+        ta, tb = int(rng.integers(0, 2)), int(rng.integers(0, 2))
+        A = rng.standard_normal((K, M) if ta else (M, K)).astype(np.float32)
+        B = rng.standard_normal((N, K) if tb else (K, N)).astype(np.float32)
+        C0 = rng.standard_normal((M, N)).astype(np.float32)
+        alpha, beta = (1.0, 0.0) if not with_epilogue else (float(rng.choice([1.0, 0.5])), float(rng.choice([0.0, 2.0])))
+        bias = rng.standard_normal(N).astype(np.float32) if with_epilogue and i % 2 else None
+        act = int(rng.integers(0, 3)) if with_epilogue else 0
+        mask = rng.standard_normal((M, N)).astype(np.float32) if with_epilogue and i % 3 == 0 else None
+        host.append((ta, tb, M, N, K, alpha, beta, A, B, C0, bias, act, mask))
+        specs.append((ta, tb, M, N, K, alpha, beta, vk.Array(gpu, data=A), vk.Array(gpu, data=B),
+                      vk.Array(gpu, data=C0), None if bias is None else vk.Array(gpu, data=bias), act,
+                      None if mask is None else vk.Array(gpu, data=mask)))
+    return specs, host
+
+
+def _expected(h):
+    ta, tb, M, N, K, alpha, beta, A, B, C0, bias, act, mask = h
+    opA = A.T if ta else A
+    opB = B.T if tb else B
+    v = alpha * (opA.astype(np.float64) @ opB.astype(np.float64)) + beta * C0
+    if bias is not None:
+        v = v + bias
+    if act == 1:
+        v = np.maximum(v, 0)
+    elif act == 2:
+        v = 1 / (1 + np.exp(-v))
+    if mask is not None:
+        v = v * (mask > 0)
+    return v
+
+
+def _single(vk, gpu, lib_, prec, spec):
+    """The same problem through vkc_gemm (+ the separate ReLU-backward kernel
+    for a mask) -- the per-op path the grouped call must reproduce."""
+    ta, tb, M, N, K, alpha, beta, A, B, C0, bias, act, mask = spec
+    assert bias is None and act == 0 and mask is None
+    c = vk.Array(gpu, data=np.zeros((M, N), np.float32))
+    st = lib_.lib.vkc_gemm(gpu.handle, prec, ta, tb, M, N, K, C.c_float(alpha), A._dptr() if K else None,
+                           (M if ta else K), B._dptr() if K else None, (K if tb else N), C.c_float(beta), c._dptr(), N)
+    assert st == 0, lib_.last_error()
+    c._written()
+    return np.asarray(c).copy()
+
+
+@pytest.mark.parametrize("prec_name,bound", [("fp32", 2e-6), ("bf16x3", 1e-5), ("bf16", 8e-3)])
+def test_grouped_accuracy_and_epilogue(gpu, vk, prec_name, bound):
+    from vulkpy_gb300 import _lib as lib_
+    prec = {"fp32": lib_.MM_FP32, "bf16": lib_.MM_BF16, "bf16x3": lib_.MM_BF16X3}[prec_name]
+    rng = np.random.default_rng(11)
+    specs, host = _specs(vk, gpu, rng, 24, with_epilogue=True)
+    got = _run_grouped(vk, gpu, lib_, prec, specs)
+    for g, h in zip(got, host):
+        e = _expected(h)
+        if e.size == 0:
+            continue
+        assert rel_fro(g, e) < bound, (prec_name, h[2:5], rel_fro(g, e))
+    assert gpu.check_errors() == 0
+
+
+@pytest.mark.parametrize("prec_name", ["fp32", "bf16x3"])
+def test_grouped_bit_identical_to_single(gpu, vk, prec_name):
+    from vulkpy_gb300 import _lib as lib_, autotune
+    prec = {"fp32": lib_.MM_FP32, "bf16x3": lib_.MM_BF16X3}[prec_name]
+    rng = np.random.default_rng(5)
+    specs, host = _specs(vk, gpu, rng, 20, with_epilogue=False)
+    # the single-problem path must not split K for a bit-for-bit comparison
+    for s in specs:
+        assert lib_.lib.vkc_gemm_tune_set(lib_.MM_BF16X3, s[2], s[3], s[4], 1) == 0
+    try:
+        fresh = [(ta, tb, M, N, K, a, b, A, B, vk.Array(gpu, data=np.zeros((M, N), np.float32)), bias, act, mask)
+                 for (ta, tb, M, N, K, a, b, A, B, C0, bias, act, mask) in specs]
+        got = _run_grouped(vk, gpu, lib_, prec, fresh)
+        for g, s in zip(got, specs):
+            np.testing.assert_array_equal(g, _single(vk, gpu, lib_, prec, s), err_msg=str(s[2:5]))
+    finally:
+        lib_.lib.vkc_gemm_tune_clear()
+        autotune.load_table()
+    assert gpu.check_errors() == 0
+
+
+def test_matmul_grouped_api(gpu, vk):
+    rng = np.random.default_rng(2)
+    As = [rng.standard_normal((m, k)).astype(np.float32) for m, k in [(3, 5), (64, 200), (130, 17)]]
+    Bs = [rng.standard_normal((k, n)).astype(np.float32) for k, n in [(5, 9), (200, 1), (17, 300)]]
+    for prec, bound in (("fp32", 1e-6), ("bf16x3", 1e-5)):
+        outs = vk.vkarray.matmul_grouped([vk.Array(gpu, data=a) for a in As], [vk.Array(gpu, data=b) for b in Bs],
+                                         precision=prec)
+        for o, a, b in zip(outs, As, Bs):
+            assert rel_fro(np.asarray(o), a.astype(np.float64) @ b) < bound
+    with pytest.raises(ValueError):
+        vk.vkarray.matmul_grouped([vk.Array(gpu, data=As[0])], [vk.Array(gpu, data=Bs[1])])
+
+
+def _models(vk, gpu, dims, seed0=7):
+    nn = vk.nn
+    out = []
+    for k, (i, h, o, b) in enumerate(dims):
+        opt = nn.SGD(lr=1e-2)
+        out.append(nn.Sequence([
+            nn.Dense(gpu, i, h, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, i, seed=seed0 + k)), nn.ReLU(),
+            nn.Dense(gpu, h, o, w_opt=opt, b_opt=opt, w_init=nn.HeNormal(gpu, h, seed=seed0 + 1000 + k)),
+        ], nn.MSELoss()))
+    return out
+
+
+def _params(models):
+    return [np.asarray(p.value).copy() for m in models for d in (m.L[0], m.L[2]) for p in (d.w, d.b)]
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16x3"])
+def test_grouped_sequence_matches_per_model_training(gpu, vk, prec):
+    from vulkpy_gb300 import _lib as lib_, autotune
+    rng = np.random.default_rng(2)
+    dims = [(int(rng.integers(17, 1022)), int(rng.integers(32, 2049)), int(rng.integers(2, 65)),
+             int(rng.integers(1, 513))) for _ in range(10)]
+    data = [(rng.standard_normal((b, i)).astype(np.float32), rng.standard_normal((b, o)).astype(np.float32))
+            for i, h, o, b in dims]
+    xs = [vk.Array(gpu, data=x) for x, _ in data]
+    ys = [vk.Array(gpu, data=y) for _, y in data]
+    old = gpu.matmul_precision
+    gpu.matmul_precision = prec
+    # the per-model path must not split K (for bit-identity of the x3 sums)
+    for (i, h, o, b) in dims:
+        for (m, n, k) in ((b, h, i), (b, o, h), (o, h, b), (h, i, b), (b, h, o)):
+            lib_.lib.vkc_gemm_tune_set(lib_.MM_BF16X3, m, n, k, 1)
+    try:
+        ref = _models(vk, gpu, dims)
+        ref_losses = []
+        for step in range(3):
+            ref_losses.append([float(np.asarray(m.train(x, y)[1])[0]) for m, x, y in zip(ref, xs, ys)])
+        grp_models = _models(vk, gpu, dims)
+        grp = vk.nn.GroupedSequence(grp_models)
+        grp_losses = []
+        for step in range(3):
+            preds, losses = grp.train(xs, ys)
+            grp_losses.append(np.asarray(losses).tolist())
+        for a, b in zip(_params(ref), _params(grp_models)):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_allclose(np.array(grp_losses), np.array(ref_losses), rtol=2e-6)
+
+        # one captured step, replayed, continues exactly like eager steps
+        g = vk.graph.Graph(gpu)
+        with g:
+            preds, losses = grp.train(xs, ys)
+        for _ in range(2):
+            g.launch()
+            for m, x, y in zip(ref, xs, ys):
+                m.train(x, y)
+        for a, b in zip(_params(ref), _params(grp_models)):
+            np.testing.assert_array_equal(a, b)
+    finally:
+        gpu.matmul_precision = old
+        lib_.lib.vkc_gemm_tune_clear()
+        autotune.load_table()
+    assert gpu.check_errors() == 0
+
+
+def test_grouped_sequence_rejects_unsupported(gpu, vk):
+    nn = vk.nn
+    a = nn.Sequence([nn.Dense(gpu, 3, 4), nn.ReLU(), nn.Dense(gpu, 4, 2)], nn.MSELoss())
+    b = nn.Sequence([nn.Dense(gpu, 3, 2)], nn.MSELoss())
+    with pytest.raises(ValueError):
+        nn.GroupedSequence([a, b])                       # different layer patterns
+    with pytest.raises(NotImplementedError):
+        nn.GroupedSequence([nn.Sequence([nn.Dense(gpu, 3, 2)], nn.CrossEntropyLoss())])
+    with pytest.raises(NotImplementedError):
+        nn.GroupedSequence([nn.Sequence([nn.Dense(gpu, 3, 2, w_opt=nn.Adam(gpu), b_opt=nn.Adam(gpu))],
+                                        nn.MSELoss())])

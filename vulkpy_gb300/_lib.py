@@ -43,6 +43,15 @@ f64 = C.c_double
 u32 = C.c_uint32
 u64 = C.c_uint64
 pi64 = C.POINTER(C.c_int64)
+pvp = C.POINTER(C.c_void_p)
+
+
+class GemmProblem(C.Structure):
+    """struct vkc_gemm_problem (include/vulkpy_gb300.h)."""
+    _fields_ = [("ta", C.c_int32), ("tb", C.c_int32), ("m", C.c_int64), ("n", C.c_int64), ("k", C.c_int64),
+                ("alpha", C.c_float), ("beta", C.c_float), ("a", C.c_void_p), ("lda", C.c_int64),
+                ("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p), ("ldc", C.c_int64),
+                ("bias", C.c_void_p), ("act", C.c_int32), ("relu_mask", C.c_void_p)]
 
 _SIGS = {
     "vkc_last_error": ([], C.c_char_p),
@@ -87,6 +96,10 @@ _SIGS = {
     "vkc_gemm_tune_set": ([i32, i64, i64, i64, i32], i32),
     "vkc_gemm_tune_get": ([vp, i32, i64, i64, i64, C.POINTER(C.c_int)], i32),
     "vkc_gemm_tune_clear": ([], i32),
+    "vkc_gemm_grouped": ([vp, i32, C.POINTER(GemmProblem), i32], i32),
+    "vkc_colsum_grouped": ([vp, pvp, pvp, pi64, pi64, i32, i32], i32),
+    "vkc_sgd_update_grouped": ([vp, pvp, pvp, pi64, f64, i32], i32),
+    "vkc_mse_grouped": ([vp, pvp, pvp, pvp, pi64, pi64, vp, i32], i32),
     "vkc_gather": ([vp, vp, sz, vp, sz, vp], i32),
     "vkc_gather_axis": ([vp, vp, sz, sz, sz, vp, sz, vp], i32),
     "vkc_arg_reduce_all": ([vp, i32, vp, sz, vp], i32),

@@ -19,16 +19,31 @@ struct GemmEpilogue {
   int act = VKC_ACT_NONE;
 };
 
+struct SimtSmem {
+  float As[2][kGemmBK][kGemmBM];
+  float Bs[2][kGemmBK][kGemmBN];
+};
+
+// ReLU backward applied to a GEMM result as the separate activation-backward
+// kernel does it: v * max(sign(y), 0), one float32 multiply.
+__device__ __forceinline__ float relu_mask(float v, float y) {
+  float s = y > 0.f ? 1.f : (y < 0.f ? -1.f : y);
+  s = fmaxf(s, 0.f);
+  return __fmul_rn(s, v);
+}
+
+// One 128 x 128 output tile at (m0, n0).  `mask` (may be NULL, same layout
+// as C) multiplies the result by the ReLU derivative of mask[m, n].  The
+// caller synchronises the block before reusing `sm` for another tile.
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(kGemmThreads)
-k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restrict__ A, int64_t lda,
-            const float* __restrict__ B, int64_t ldb, float beta, float* C, int64_t ldc, GemmEpilogue epi) {
-  __shared__ __align__(16) float As[2][kGemmBK][kGemmBM];
-  __shared__ __align__(16) float Bs[2][kGemmBK][kGemmBN];
+__device__ __forceinline__ void simt_tile(int64_t M, int64_t N, int64_t K, float alpha, const float* __restrict__ A,
+                                          int64_t lda, const float* __restrict__ B, int64_t ldb, float beta, float* C,
+                                          int64_t ldc, GemmEpilogue epi, const float* __restrict__ mask, int64_t m0,
+                                          int64_t n0, SimtSmem& sm) {
+  auto& As = sm.As;
+  auto& Bs = sm.Bs;
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  const int64_t m0 = (int64_t)blockIdx.y * kGemmBM;
-  const int64_t n0 = (int64_t)blockIdx.x * kGemmBN;
 
   // Each thread loads 4 elements of the A tile and 4 of the B tile per K step.
   // op(A)(m,k) = TA ? A[k*lda + m] : A[m*lda + k]; op(B)(k,n) = TB ? B[n*ldb + k] : B[k*ldb + n].
@@ -115,9 +130,19 @@ k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restric
       if (epi.bias) v += epi.bias[gn];
       if (epi.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
       else if (epi.act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+      if (mask) v = relu_mask(v, mask[gm * ldc + gn]);
       C[gm * ldc + gn] = v;
     }
   }
+}
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(kGemmThreads)
+k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restrict__ A, int64_t lda,
+            const float* __restrict__ B, int64_t ldb, float beta, float* C, int64_t ldc, GemmEpilogue epi) {
+  __shared__ __align__(16) SimtSmem sm;
+  simt_tile<TA, TB>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi, nullptr, (int64_t)blockIdx.y * kGemmBM,
+                    (int64_t)blockIdx.x * kGemmBN, sm);
 }
 
 inline int gemm_simt(vkc_device_t dev, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,

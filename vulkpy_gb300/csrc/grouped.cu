@@ -1,0 +1,795 @@
+// Grouped GEMM: many independent problems of different shapes in one
+// persistent launch, and the grouped element-wise pieces of a batched MLP
+// training step (bias-gradient column sums, MSE loss and gradient, SGD).
+//
+// vulkpy runs every Dense layer of every model as its own job
+// (batch_affine.comp, _vkarray.cc:403-438); 64 small models of uneven sizes
+// are then bound by per-launch cost and by GEMMs too small to fill 152 SMs.
+// Here the output tiles of all problems form one work list, ordered by K
+// (longest first), and a persistent grid walks it round-robin.
+//
+// fp32: each tile is computed by the same code as the single-problem SIMT
+// kernel (simt_tile), so results are bit-identical to vkc_gemm.
+// bf16 / split-bf16x3: a pre-pass converts every operand into 128 x 64 bf16
+// tiles already laid out as the 128-byte-swizzled shared-memory image the
+// MMA descriptors expect (tile (r, k): row r's 16-byte chunk c at byte
+// r*128 + ((c ^ (r & 7)) << 4)), so one untiled bulk copy per operand tile
+// fills a pipeline stage -- no tensor maps, whose per-problem encoding would
+// not fit a launch.  The MMA and epilogue follow k_gemm_tc_x3 (one TMEM
+// buffer per 64-wide K block, drained into fp32 registers), so split-bf16x3
+// results are bit-identical to vkc_gemm when that call does not split K.
+#include "gemm_simt.cuh"
+#include "tc_ptx.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+namespace vkc {
+namespace {
+
+constexpr int kMaxGroup = 128;  // problems per launch (tables travel as kernel parameters)
+
+// ------------------------------------------------------------ fp32 SIMT
+struct SimtProb {
+  const float* a;
+  const float* b;
+  float* c;
+  const float* bias;
+  const float* mask;
+  int64_t lda, ldb, ldc;
+  int64_t m, n, k;
+  float alpha, beta;
+  int act, trans;  // trans: bit0 op(A) = A^T, bit1 op(B) = B^T
+  int tiles_n, tile0;
+};
+
+struct SimtTable {
+  int count, total;
+  SimtProb p[kMaxGroup];
+};
+
+template <class T>
+__device__ __forceinline__ int find_problem(const T* p, int count, int t) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (p[mid].tile0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_simt_grouped(const __grid_constant__ SimtTable tab) {
+  __shared__ __align__(16) SimtSmem sm;
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    const SimtProb& P = tab.p[find_problem(tab.p, tab.count, t)];
+    const int local = t - P.tile0;
+    const int64_t m0 = (int64_t)(local / P.tiles_n) * kGemmBM;
+    const int64_t n0 = (int64_t)(local % P.tiles_n) * kGemmBN;
+    GemmEpilogue epi;
+    epi.bias = P.bias;
+    epi.act = P.act;
+    __syncthreads();  // the previous tile's reads of `sm` are done
+    switch (P.trans) {
+      case 0:
+        simt_tile<false, false>(P.m, P.n, P.k, P.alpha, P.a, P.lda, P.b, P.ldb, P.beta, P.c, P.ldc, epi, P.mask, m0,
+                                n0, sm);
+        break;
+      case 1:
+        simt_tile<true, false>(P.m, P.n, P.k, P.alpha, P.a, P.lda, P.b, P.ldb, P.beta, P.c, P.ldc, epi, P.mask, m0,
+                               n0, sm);
+        break;
+      case 2:
+        simt_tile<false, true>(P.m, P.n, P.k, P.alpha, P.a, P.lda, P.b, P.ldb, P.beta, P.c, P.ldc, epi, P.mask, m0,
+                               n0, sm);
+        break;
+      default:
+        simt_tile<true, true>(P.m, P.n, P.k, P.alpha, P.a, P.lda, P.b, P.ldb, P.beta, P.c, P.ldc, epi, P.mask, m0,
+                              n0, sm);
+        break;
+    }
+  }
+}
+
+// ------------------------------------------------------------ operand tiling
+constexpr int kTileRows = 128, kTileK = 64;
+constexpr uint32_t kTileBytes = kTileRows * kTileK * 2;  // 16 KB of bf16
+
+struct TileOp {
+  const float* src;
+  __nv_bfloat16* hi;
+  __nv_bfloat16* lo;  // NULL: plain bf16
+  int64_t ld;
+  int64_t rows, k;    // logical operand: rows x k, element (r, k)
+  int k_contig;       // element (r, k) at src[r*ld + k]; else src[k*ld + r]
+  int kt;             // K tiles
+  int tile0;
+};
+
+struct TileTable {
+  int count, total;
+  TileOp op[2 * kMaxGroup];
+};
+
+// One 128 x 64 tile per block iteration: load (coalesced along whichever
+// index is contiguous) into shared memory, then write 16-byte chunks of hi
+// (and lo = bf16(x - hi)) at their swizzled positions.  Rows >= rows and
+// k >= K are written as zeros.
+__global__ void __launch_bounds__(256) k_tile_operands(const __grid_constant__ TileTable tab) {
+  __shared__ float s[kTileRows][kTileK + 1];
+  const int tid = threadIdx.x;
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    const TileOp& op = tab.op[find_problem(tab.op, tab.count, t)];
+    const int local = t - op.tile0;
+    const int rt = local / op.kt, kt = local % op.kt;
+    const int64_t r0 = (int64_t)rt * kTileRows, k0 = (int64_t)kt * kTileK;
+    __syncthreads();
+    if (op.k_contig) {
+#pragma unroll 4
+      for (int i = 0; i < kTileRows * kTileK / 256; ++i) {
+        const int e = i * 256 + tid;
+        const int r = e >> 6, k = e & 63;
+        const int64_t gr = r0 + r, gk = k0 + k;
+        s[r][k] = (gr < op.rows && gk < op.k) ? op.src[gr * op.ld + gk] : 0.f;
+      }
+    } else {
+#pragma unroll 4
+      for (int i = 0; i < kTileRows * kTileK / 256; ++i) {
+        const int e = i * 256 + tid;
+        const int k = e >> 7, r = e & 127;
+        const int64_t gr = r0 + r, gk = k0 + k;
+        s[r][k] = (gr < op.rows && gk < op.k) ? op.src[gk * op.ld + gr] : 0.f;
+      }
+    }
+    __syncthreads();
+    const size_t tile_elems = (size_t)local * (kTileRows * kTileK);
+    uint8_t* hi = reinterpret_cast<uint8_t*>(op.hi + tile_elems);
+    uint8_t* lo = op.lo ? reinterpret_cast<uint8_t*>(op.lo + tile_elems) : nullptr;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int cidx = i * 256 + tid;  // 128 rows x 8 chunks of 8 elements
+      const int r = cidx >> 3, c = cidx & 7;
+      uint32_t h[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float x0 = s[r][c * 8 + 2 * j], x1 = s[r][c * 8 + 2 * j + 1];
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
+        const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
+        const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
+        h[j] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+        l[j] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+      }
+      const size_t off = (size_t)r * 128 + (size_t)(((c ^ (r & 7)) << 4));
+      *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+      if (lo) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+  }
+}
+
+// ------------------------------------------------------------ tensor cores
+struct TcProb {
+  const uint8_t* a_hi;  // tiles of op(A): [M/128][K/64] x 16 KB
+  const uint8_t* a_lo;
+  const uint8_t* b_hi;  // tiles of op(B)^T: [N/128][K/64] x 16 KB
+  const uint8_t* b_lo;
+  float* c;
+  const float* bias;
+  const float* mask;
+  int64_t ldc;
+  int m, n, kt;  // kt: 64-wide K blocks (>= 1)
+  float alpha, beta;
+  int act, tiles_n, tile0;
+};
+
+struct TcTable {
+  int count, total;
+  TcProb p[kMaxGroup];
+};
+
+constexpr int kGroupedStages = 3;
+
+template <bool X3>
+struct GroupedCfg {
+  static constexpr uint32_t kStageBytes = (X3 ? 4u : 2u) * kTileBytes;
+  static constexpr uint32_t kBarBytes = 8u * (2 * kGroupedStages + 2 * kAccBufs + 1) + 16;
+  static constexpr uint32_t kSmem = kGroupedStages * kStageBytes + 1024 + 256;
+};
+
+// One CTA per SM walks the tile list.  The stage ring and the TMEM buffer
+// ring continue across tiles (a running K-block counter gives every slot and
+// parity), so the next tile's copies and MMAs overlap this tile's epilogue.
+template <bool X3>
+__global__ void __launch_bounds__(kThreadsTC, 1)
+k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
+  constexpr int BN = 128;
+  constexpr int S = kGroupedStages;
+  using Cfg = GroupedCfg<X3>;
+  constexpr uint32_t kCols = BN * kAccBufs;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* gbase = smem_raw + (base - raw);
+  const uint32_t bars = base + S * Cfg::kStageBytes;
+  auto full_bar = [&](int s) { return bars + 8u * s; };
+  auto empty_bar = [&](int s) { return bars + 8u * (S + s); };
+  auto accf_bar = [&](int b) { return bars + 8u * (2 * S + b); };
+  auto acce_bar = [&](int b) { return bars + 8u * (2 * S + kAccBufs + b); };
+  const uint32_t drain_bar = bars + 8u * (2 * S + 2 * kAccBufs);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + S * Cfg::kStageBytes + 8 * (2 * S + 2 * kAccBufs + 1));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < kAccBufs; ++b) {
+      mbar_init(accf_bar(b), 1);
+      mbar_init(acce_bar(b), 4);
+    }
+    mbar_init(drain_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
+
+  auto stage = [&](int s, int which) { return base + s * Cfg::kStageBytes + (uint32_t)which * kTileBytes; };
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- bulk-copy producer
+    uint32_t g = 0, issued_from = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
+      const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
+      const int local = t - P.tile0;
+      const size_t a_off = (size_t)(local / P.tiles_n) * P.kt * kTileBytes;
+      const size_t b_off = (size_t)(local % P.tiles_n) * P.kt * kTileBytes;
+      for (int kb = 0; kb < P.kt; ++kb, ++g) {
+        const int s = g % S;
+        if (*abort_flag || !mbar_wait(empty_bar(s), ((g / S) & 1) ^ 1)) { ok = false; break; }
+        mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
+        const size_t kofs = (size_t)kb * kTileBytes;
+        bulk_load(stage(s, 0), P.a_hi + a_off + kofs, kTileBytes, full_bar(s));
+        bulk_load(stage(s, 1), P.b_hi + b_off + kofs, kTileBytes, full_bar(s));
+        if (X3) {
+          bulk_load(stage(s, 2), P.a_lo + a_off + kofs, kTileBytes, full_bar(s));
+          bulk_load(stage(s, 3), P.b_lo + b_off + kofs, kTileBytes, full_bar(s));
+        }
+      }
+    }
+    if (!ok) {
+      atomicOr(err, 2u);
+      *abort_flag = 1;
+      // drain the copies still in flight into this CTA's shared memory
+      issued_from = g > (uint32_t)S ? g - S : 0;
+      for (uint32_t q = issued_from; q < g; ++q) mbar_wait(full_bar(q % S), (q / S) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                               ((uint32_t)(kTileRows >> 4) << 24);
+    uint32_t g = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
+      const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
+      for (int kb = 0; kb < P.kt; ++kb, ++g) {
+        const int s = g % S, b = g % kAccBufs;
+        if (*abort_flag || !mbar_wait(full_bar(s), (g / S) & 1) ||
+            !mbar_wait(acce_bar(b), ((g / kAccBufs) & 1) ^ 1)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+#pragma unroll
+        for (int k = 0; k < kTileK / 16; ++k) {
+          const uint64_t a = sw128_desc(stage(s, 0) + 32u * k);
+          const uint64_t bb = sw128_desc(stage(s, 1) + 32u * k);
+          if (X3) {
+            // the same order as k_gemm_tc_x3: cross terms, then hi*hi
+            mma_bf16(d, a, sw128_desc(stage(s, 3) + 32u * k), idesc, k != 0);
+            mma_bf16(d, sw128_desc(stage(s, 2) + 32u * k), bb, idesc, 1);
+            mma_bf16(d, a, bb, idesc, 1);
+          } else {
+            mma_bf16(d, a, bb, idesc, k != 0);
+          }
+        }
+        mma_commit(empty_bar(s));
+        mma_commit(accf_bar(b));
+      }
+    }
+    if (!ok) {
+      atomicOr(err, 2u);
+      *abort_flag = 1;
+    }
+  } else if (warp >= 2) {
+    // ---------------- epilogue: drain every K block into fp32 registers
+    const int q = warp & 3;
+    uint32_t g = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
+      const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
+      const int local = t - P.tile0;
+      const int m0 = (local / P.tiles_n) * kTileRows, n0 = (local % P.tiles_n) * BN;
+      float sum[BN];
+#pragma unroll
+      for (int j = 0; j < BN; ++j) sum[j] = 0.f;
+      for (int kb = 0; kb < P.kt; ++kb, ++g) {
+        const int b = g % kAccBufs;
+        if (*abort_flag || !mbar_wait(accf_bar(b), (g / kAccBufs) & 1)) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll
+        for (int c = 0; c < BN / 32; ++c) {
+          uint32_t r[32];
+          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c * 32), r);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) sum[c * 32 + j] += __uint_as_float(r[j]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce_bar(b));
+      }
+      if (!ok) break;
+      const int row = m0 + q * 32 + lane;
+      if (row < P.m) {
+        float* crow = P.c + (int64_t)row * P.ldc;
+        const float* mrow = P.mask ? P.mask + (int64_t)row * P.ldc : nullptr;
+#pragma unroll
+        for (int j = 0; j < BN; ++j) {  // fully unrolled: sum[] stays in registers
+          const int col = n0 + j;
+          if (col < P.n) {
+            float v = P.alpha * sum[j];
+            if (P.beta != 0.f) v += P.beta * crow[col];
+            if (P.bias) v += P.bias[col];
+            if (P.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+            else if (P.act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+            if (mrow) v = relu_mask(v, mrow[col]);
+            crow[col] = v;
+          }
+        }
+      }
+    }
+    if (!ok) {
+      if (lane == 0) atomicOr(err, 2u);
+      *abort_flag = 1;
+    }
+  }
+
+  // Every MMA must have completed before TMEM is released: on the normal path
+  // the epilogue consumed every commit; after an abort the issuer commits once
+  // more and waits (bounded) for it.
+  if (warp == 1 && lane == 0 && *abort_flag) {
+    mma_commit(drain_bar);
+    mbar_wait(drain_bar, 0);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+  }
+}
+
+// ------------------------------------------------------------ MLP pieces
+struct ColsumItem {
+  const float* dy;
+  float* db;
+  int64_t batch, cols;
+  int block0;  // first block of this item (blocks of 256 columns)
+};
+struct ColsumTable {
+  int count, total, overwrite;
+  ColsumItem it[kMaxGroup];
+};
+
+// db[o] += sum_b dy[b, o], b in order: the arithmetic of the single-layer
+// bias-gradient kernel.  `overwrite`: db[o] = the sum, which equals adding it
+// to a zeroed gradient (the sum starts at +0, so it is never -0).
+__global__ void __launch_bounds__(256) k_colsum_grouped(const __grid_constant__ ColsumTable tab) {
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    int lo = 0, hi = tab.count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab.it[mid].block0 <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const ColsumItem& I = tab.it[lo];
+    const int64_t o = (int64_t)(t - I.block0) * 256 + threadIdx.x;
+    if (o < I.cols) {
+      float s = 0.f;
+#pragma unroll 8
+      for (int64_t b = 0; b < I.batch; ++b) s += I.dy[b * I.cols + o];  // loads run ahead, adds in order
+      I.db[o] = tab.overwrite ? s : I.db[o] + s;
+    }
+  }
+}
+
+struct VecItem {
+  float* value;        // SGD: parameter; MSE: gradient output
+  const float* grad;   // SGD: gradient;  MSE: prediction x
+  const float* y;      // MSE target
+  int64_t n;
+  int64_t cols;        // MSE row length
+  float scale;         // SGD: -lr; MSE: float32(1 / batch)
+  float* loss;         // MSE: per-row losses (batch floats), may be NULL
+  int block0;
+};
+struct VecTable {
+  int count, total;
+  VecItem it[2 * kMaxGroup];
+};
+
+constexpr int kVecChunk = 4096;  // elements per block iteration
+
+__device__ __forceinline__ int find_vec(const VecTable& tab, int t) {
+  int lo = 0, hi = tab.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tab.it[mid].block0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// value += (-lr) * grad, as the single-tensor SGD kernel computes it.
+__global__ void __launch_bounds__(256) k_sgd_grouped(const __grid_constant__ VecTable tab) {
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    const VecItem& I = tab.it[find_vec(tab, t)];
+    const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
+    const int64_t i1 = min(i0 + kVecChunk, I.n);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) I.value[i] = __fadd_rn(I.value[i], __fmul_rn(I.scale, I.grad[i]));
+  }
+}
+
+// MSE gradient of the mean-reduced loss: ((x - y) * 2) * float32(1/batch),
+// the three float32 operations of MSELoss.backward and ReduceLoss.grad.
+__global__ void __launch_bounds__(256) k_mse_grad_grouped(const __grid_constant__ VecTable tab) {
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    const VecItem& I = tab.it[find_vec(tab, t)];
+    const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
+    const int64_t i1 = min(i0 + kVecChunk, I.n);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256)
+      I.value[i] = __fmul_rn(__fmul_rn(__fsub_rn(I.grad[i], I.y[i]), 2.0f), I.scale);
+  }
+}
+
+// MSE loss per model: mean over rows of sum over columns of (y - x)^2.  One
+// block per model; rows summed sequentially by column, the per-row sums
+// combined in a fixed tree.  (Not the order of the per-op path, whose
+// reduction kernels depend on the shape; the value agrees to rounding.)
+__global__ void __launch_bounds__(256) k_mse_loss_grouped(const __grid_constant__ VecTable tab, float* out) {
+  __shared__ float part[256];
+  const VecItem& I = tab.it[blockIdx.x];
+  const int64_t rows = I.n / I.cols;
+  float acc = 0.f;
+  for (int64_t r = threadIdx.x; r < rows; r += 256) {
+    float s = 0.f;
+    for (int64_t c = 0; c < I.cols; ++c) {
+      const float d = __fsub_rn(I.y[r * I.cols + c], I.grad[r * I.cols + c]);
+      s = __fadd_rn(s, __fmul_rn(d, d));
+    }
+    acc += s;
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = part[0] * I.scale;
+}
+
+}  // namespace
+}  // namespace vkc
+
+using namespace vkc;
+
+// ------------------------------------------------------------ host side
+namespace {
+
+int check_problem(const vkc_gemm_problem& p, int i) {
+  if (p.m < 0 || p.n < 0 || p.k < 0) return set_error(VKC_ERR_INVALID, "grouped gemm: problem %d has a negative size", i);
+  if (p.m == 0 || p.n == 0) return VKC_OK;
+  if (!p.c || (p.k > 0 && (!p.a || !p.b)))
+    return set_error(VKC_ERR_INVALID, "grouped gemm: problem %d has a NULL buffer", i);
+  if (p.m >= (1ll << 31) || p.n >= (1ll << 31) || p.k >= (1ll << 31))
+    return set_error(VKC_ERR_INVALID, "grouped gemm: problem %d dimension too large", i);
+  if (p.act != VKC_ACT_NONE && p.act != VKC_ACT_RELU && p.act != VKC_ACT_SIGMOID)
+    return set_error(VKC_ERR_INVALID, "grouped gemm: problem %d has unknown activation %d", i, p.act);
+  return VKC_OK;
+}
+
+// Order (longest K first) of the problems that have work.
+std::vector<int> work_order(const vkc_gemm_problem* probs, int count) {
+  std::vector<int> idx;
+  for (int i = 0; i < count; ++i)
+    if (probs[i].m > 0 && probs[i].n > 0) idx.push_back(i);
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return probs[x].k > probs[y].k; });
+  return idx;
+}
+
+int grouped_simt(vkc_device_t dev, const vkc_gemm_problem* probs, const std::vector<int>& order) {
+  for (size_t s = 0; s < order.size(); s += kMaxGroup) {
+    SimtTable tab{};
+    int total = 0;
+    const size_t e = std::min(order.size(), s + kMaxGroup);
+    for (size_t j = s; j < e; ++j) {
+      const vkc_gemm_problem& q = probs[order[j]];
+      SimtProb& P = tab.p[tab.count++];
+      P.a = q.a;
+      P.b = q.b;
+      P.c = q.c;
+      P.bias = q.bias;
+      P.mask = q.relu_mask;
+      P.lda = q.lda;
+      P.ldb = q.ldb;
+      P.ldc = q.ldc;
+      P.m = q.m;
+      P.n = q.n;
+      P.k = q.k;
+      P.alpha = q.alpha;
+      P.beta = q.beta;
+      P.act = q.act;
+      P.trans = (q.ta ? 1 : 0) | (q.tb ? 2 : 0);
+      P.tiles_n = (int)((q.n + kGemmBN - 1) / kGemmBN);
+      P.tile0 = total;
+      const int64_t tiles = ((q.m + kGemmBM - 1) / kGemmBM) * P.tiles_n;
+      if (total + tiles >= (1ll << 31)) return set_error(VKC_ERR_INVALID, "grouped gemm: too many tiles");
+      total += (int)tiles;
+    }
+    tab.total = total;
+    if (total == 0) continue;
+    const unsigned grid = wave_grid(dev, k_gemm_simt_grouped, (size_t)total * kGemmThreads, kGemmThreads);
+    k_gemm_simt_grouped<<<grid, kGemmThreads, 0, dev->stream>>>(tab);
+    int r = check_launch("gemm_grouped (fp32)");
+    if (r != VKC_OK) return r;
+  }
+  return VKC_OK;
+}
+
+int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const std::vector<int>& order) {
+  for (size_t s = 0; s < order.size(); s += kMaxGroup) {
+    const size_t e = std::min(order.size(), s + kMaxGroup);
+    // operand tile buffers: one allocation for the chunk
+    std::vector<size_t> a_off, b_off;
+    size_t bytes = 0;
+    for (size_t j = s; j < e; ++j) {
+      const vkc_gemm_problem& q = probs[order[j]];
+      const size_t kt = (size_t)((q.k + kTileK - 1) / kTileK);
+      const size_t at = (size_t)((q.m + kTileRows - 1) / kTileRows) * kt;
+      const size_t bt = (size_t)((q.n + kTileRows - 1) / kTileRows) * kt;
+      a_off.push_back(bytes);
+      bytes += at * kTileBytes * (x3 ? 2 : 1);
+      b_off.push_back(bytes);
+      bytes += bt * kTileBytes * (x3 ? 2 : 1);
+    }
+    void* scratch = nullptr;
+    int r = scratch_alloc(dev, bytes, &scratch);
+    if (r != VKC_OK) return r;
+    uint8_t* sbase = static_cast<uint8_t*>(scratch);
+
+    TileTable tt{};
+    TcTable tab{};
+    int ttotal = 0, total = 0;
+    for (size_t j = s; j < e; ++j) {
+      const vkc_gemm_problem& q = probs[order[j]];
+      const int kt = (int)((q.k + kTileK - 1) / kTileK);
+      const int mt = (int)((q.m + kTileRows - 1) / kTileRows), nt = (int)((q.n + kTileRows - 1) / kTileRows);
+      uint8_t* a_hi = sbase + a_off[j - s];
+      uint8_t* a_lo = x3 ? a_hi + (size_t)mt * kt * kTileBytes : nullptr;
+      uint8_t* b_hi = sbase + b_off[j - s];
+      uint8_t* b_lo = x3 ? b_hi + (size_t)nt * kt * kTileBytes : nullptr;
+      // op(A)(m, k): ta ? A[k*lda + m] : A[m*lda + k]  -> K contiguous iff !ta
+      TileOp& oa = tt.op[tt.count++];
+      oa.src = q.a;
+      oa.hi = reinterpret_cast<__nv_bfloat16*>(a_hi);
+      oa.lo = reinterpret_cast<__nv_bfloat16*>(a_lo);
+      oa.ld = q.lda;
+      oa.rows = q.m;
+      oa.k = q.k;
+      oa.k_contig = q.ta ? 0 : 1;
+      oa.kt = kt;
+      oa.tile0 = ttotal;
+      ttotal += mt * kt;
+      // op(B)^T(n, k): tb ? B[n*ldb + k] : B[k*ldb + n]  -> K contiguous iff tb
+      TileOp& ob = tt.op[tt.count++];
+      ob.src = q.b;
+      ob.hi = reinterpret_cast<__nv_bfloat16*>(b_hi);
+      ob.lo = reinterpret_cast<__nv_bfloat16*>(b_lo);
+      ob.ld = q.ldb;
+      ob.rows = q.n;
+      ob.k = q.k;
+      ob.k_contig = q.tb ? 1 : 0;
+      ob.kt = kt;
+      ob.tile0 = ttotal;
+      ttotal += nt * kt;
+
+      TcProb& P = tab.p[tab.count++];
+      P.a_hi = a_hi;
+      P.a_lo = a_lo;
+      P.b_hi = b_hi;
+      P.b_lo = b_lo;
+      P.c = q.c;
+      P.bias = q.bias;
+      P.mask = q.relu_mask;
+      P.ldc = q.ldc;
+      P.m = (int)q.m;
+      P.n = (int)q.n;
+      P.kt = kt;
+      P.alpha = q.alpha;
+      P.beta = q.beta;
+      P.act = q.act;
+      P.tiles_n = nt;
+      P.tile0 = total;
+      total += mt * nt;
+    }
+    tt.total = ttotal;
+    tab.total = total;
+    const unsigned tgrid = wave_grid(dev, k_tile_operands, (size_t)ttotal * 256, 256);
+    k_tile_operands<<<tgrid, 256, 0, dev->stream>>>(tt);
+    r = check_launch("gemm_grouped tiling");
+    if (r == VKC_OK) {
+      const unsigned grid = (unsigned)std::min<int>(total, dev->sm_count);
+      if (x3) {
+        static bool attr = false;
+        if (!attr) {
+          cudaFuncSetAttribute(k_gemm_tc_grouped<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               GroupedCfg<true>::kSmem);
+          attr = true;
+        }
+        k_gemm_tc_grouped<true><<<grid, kThreadsTC, GroupedCfg<true>::kSmem, dev->stream>>>(tab, dev->err_word);
+      } else {
+        static bool attr = false;
+        if (!attr) {
+          cudaFuncSetAttribute(k_gemm_tc_grouped<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               GroupedCfg<false>::kSmem);
+          attr = true;
+        }
+        k_gemm_tc_grouped<false><<<grid, kThreadsTC, GroupedCfg<false>::kSmem, dev->stream>>>(tab, dev->err_word);
+      }
+      r = check_launch("gemm_grouped (tensor cores)");
+    }
+    scratch_free(dev, scratch);
+    if (r != VKC_OK) return r;
+  }
+  return VKC_OK;
+}
+
+}  // namespace
+
+VKC_EXPORT int vkc_gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_problem* problems, int count) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(count >= 0, "negative problem count");
+  if (count == 0) return VKC_OK;
+  VKC_REQUIRE(problems, "problems is NULL");
+  VKC_REQUIRE(precision == VKC_MM_FP32 || precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3,
+              "unknown matmul precision %d", precision);
+  for (int i = 0; i < count; ++i) {
+    int r = check_problem(problems[i], i);
+    if (r != VKC_OK) return r;
+  }
+  std::vector<int> order = work_order(problems, count);
+  if (precision == VKC_MM_FP32) return grouped_simt(dev, problems, order);
+  // K = 0 has no tensor-core work: C = act(beta*C + bias) through the SIMT path
+  std::vector<int> tc, simt;
+  for (int i : order) (problems[i].k > 0 ? tc : simt).push_back(i);
+  int r = grouped_simt(dev, problems, simt);
+  if (r != VKC_OK) return r;
+  return grouped_tc(dev, precision == VKC_MM_BF16X3, problems, tc);
+}
+
+VKC_EXPORT int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
+                                  const int64_t* cols, int count, int overwrite) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(count >= 0, "negative item count");
+  if (count == 0) return VKC_OK;
+  VKC_REQUIRE(dy && db && batch && cols, "NULL argument");
+  for (int s = 0; s < count; s += kMaxGroup) {
+    ColsumTable tab{};
+    tab.overwrite = overwrite ? 1 : 0;
+    int total = 0;
+    for (int i = s; i < std::min(count, s + kMaxGroup); ++i) {
+      VKC_REQUIRE(batch[i] >= 0 && cols[i] >= 0, "negative size");
+      if (cols[i] == 0 || (batch[i] == 0 && !overwrite)) continue;
+      VKC_REQUIRE((dy[i] || batch[i] == 0) && db[i], "NULL buffer");
+      ColsumItem& I = tab.it[tab.count++];
+      I.dy = dy[i];
+      I.db = db[i];
+      I.batch = batch[i];
+      I.cols = cols[i];
+      I.block0 = total;
+      total += (int)((cols[i] + 255) / 256);
+    }
+    tab.total = total;
+    if (total == 0) continue;
+    k_colsum_grouped<<<(unsigned)std::min<int>(total, dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
+    int r = check_launch("colsum_grouped");
+    if (r != VKC_OK) return r;
+  }
+  return VKC_OK;
+}
+
+namespace {
+int vec_launch(vkc_device_t dev, int kind, float* const* value, const float* const* grad, const float* const* y,
+               const int64_t* n, const int64_t* cols, const float* scale, int count, float* loss_out) {
+  for (int s = 0; s < count; s += 2 * kMaxGroup) {
+    VecTable tab{};
+    int total = 0;
+    const int e = std::min(count, s + 2 * kMaxGroup);
+    for (int i = s; i < e; ++i) {
+      VKC_REQUIRE(n[i] >= 0, "negative size");
+      if (n[i] == 0 && kind != 2) continue;
+      VecItem& I = tab.it[tab.count++];
+      I.value = value ? value[i] : nullptr;
+      I.grad = grad[i];
+      I.y = y ? y[i] : nullptr;
+      I.n = n[i];
+      I.cols = cols ? cols[i] : 1;
+      I.scale = scale[i];
+      I.block0 = total;
+      total += (int)((n[i] + kVecChunk - 1) / kVecChunk);
+    }
+    tab.total = total;
+    if (tab.count == 0) continue;
+    if (kind == 0) {
+      k_sgd_grouped<<<(unsigned)std::min<int>(std::max(total, 1), dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
+    } else if (kind == 1) {
+      k_mse_grad_grouped<<<(unsigned)std::min<int>(std::max(total, 1), dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
+    } else {
+      k_mse_loss_grouped<<<(unsigned)tab.count, 256, 0, dev->stream>>>(tab, loss_out + s);
+    }
+    int r = check_launch("grouped vector op");
+    if (r != VKC_OK) return r;
+  }
+  return VKC_OK;
+}
+}  // namespace
+
+VKC_EXPORT int vkc_sgd_update_grouped(vkc_device_t dev, float* const* value, const float* const* grad,
+                                      const int64_t* n, double lr, int count) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(count >= 0, "negative item count");
+  if (count == 0) return VKC_OK;
+  VKC_REQUIRE(value && grad && n, "NULL argument");
+  for (int i = 0; i < count; ++i) VKC_REQUIRE(n[i] == 0 || (value[i] && grad[i]), "NULL buffer");
+  std::vector<float> scale((size_t)count, (float)(-lr));
+  return vec_launch(dev, 0, value, grad, nullptr, n, nullptr, scale.data(), count, nullptr);
+}
+
+VKC_EXPORT int vkc_mse_grouped(vkc_device_t dev, const float* const* x, const float* const* y, float* const* dx,
+                               const int64_t* batch, const int64_t* cols, float* loss, int count) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(count >= 0, "negative item count");
+  if (count == 0) return VKC_OK;
+  VKC_REQUIRE(x && y && batch && cols, "NULL argument");
+  VKC_REQUIRE(count <= 2 * kMaxGroup || !loss, "grouped MSE loss: at most %d models per call", 2 * kMaxGroup);
+  std::vector<int64_t> n((size_t)count);
+  std::vector<float> scale((size_t)count);
+  for (int i = 0; i < count; ++i) {
+    VKC_REQUIRE(batch[i] > 0 && cols[i] > 0, "grouped MSE: empty model %d", i);
+    VKC_REQUIRE(x[i] && y[i], "NULL buffer");
+    n[i] = batch[i] * cols[i];
+    scale[i] = (float)(1.0 / (double)batch[i]);
+  }
+  int r = VKC_OK;
+  if (dx) {
+    for (int i = 0; i < count; ++i) VKC_REQUIRE(dx[i], "NULL buffer");
+    r = vec_launch(dev, 1, dx, x, y, n.data(), cols, scale.data(), count, nullptr);
+  }
+  if (r == VKC_OK && loss) r = vec_launch(dev, 2, nullptr, x, y, n.data(), cols, scale.data(), count, loss);
+  return r;
+}

@@ -34,7 +34,8 @@ __global__ void k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, fl
   int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= out_dim) return;
   float s = 0.f;
-  for (int64_t b = 0; b < batch; ++b) s += dy[b * out_dim + o];
+#pragma unroll 8
+  for (int64_t b = 0; b < batch; ++b) s += dy[b * out_dim + o];  // loads run ahead, adds in order
   db[o] += s;
 }
 

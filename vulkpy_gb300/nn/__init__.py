@@ -18,3 +18,4 @@ from .regularizers import Lasso, Ridge, Elastic
 from .models import Sequence
 from .parameters import Parameter
 from .data import minibatches
+from .grouped import GroupedSequence

@@ -26,7 +26,7 @@ import ctypes as C
 import logging
 import os
 import threading
-from typing import Iterable, List, Optional, Tuple, Union
+from typing import Iterable, List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 
@@ -936,6 +936,37 @@ def matmul(a: Array, b: Array, precision: Optional[str] = None) -> Array:
         return a @ b
     finally:
         a._gpu.matmul_precision = old
+
+
+def matmul_grouped(a_list: Sequence["Array"], b_list: Sequence["Array"], precision: Optional[str] = None) -> List[Array]:
+    """``[a @ b for a, b in zip(a_list, b_list)]`` for 2-D operands of any
+    sizes, computed by one grouped launch (per 128 products) instead of one
+    launch per product.  ``precision`` as for ``matmul`` (default: the GPU's
+    ``matmul_precision``).  No counterpart in the reference."""
+    if len(a_list) != len(b_list):
+        raise ValueError("a_list and b_list differ in length")
+    if not a_list:
+        return []
+    gpu = a_list[0]._gpu
+    prec = precision or gpu.matmul_precision
+    if prec not in _MATMUL_PRECISION:
+        raise ValueError(f"unknown matmul precision {prec!r}")
+    probs, outs = [], []
+    for a, b in zip(a_list, b_list):
+        if len(a.shape) != 2 or len(b.shape) != 2 or a.shape[1] != b.shape[0]:
+            raise ValueError(f"Incompatible shapes for grouped matmul: {a.shape} @ {b.shape}")
+        m, k = a.shape
+        n = b.shape[1]
+        c = Array(gpu, shape=(m, n))
+        outs.append(c)
+        probs.append(_lib.GemmProblem(ta=0, tb=0, m=m, n=n, k=k, alpha=1.0, beta=0.0, a=a._dptr(), lda=k,
+                                      b=b._dptr(), ldb=n, c=c._buf.ptr or 0, ldc=n, bias=None,
+                                      act=_lib.ACT_NONE, relu_mask=None))
+    arr = (_lib.GemmProblem * len(probs))(*probs)
+    check(lib.vkc_gemm_grouped(gpu._dev.h, _MATMUL_PRECISION[prec], arr, len(probs)))
+    for c in outs:
+        c._written()
+    return outs
 
 
 def _pad(shape, nd) -> tuple:
