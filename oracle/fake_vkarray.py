@@ -140,6 +140,23 @@ def _bcast_index3(ci, shapes, sizes, ndim):
     return ab
 
 
+def _bcast_views(shapes, ndim, a, b):
+    """When every operand dim is 1 or the output's, add_broadcast.comp's
+    index sum_k stride_k * min(d_k, s_k - 1) is exactly numpy broadcasting:
+    return the operands as broadcast views of the output shape (None when
+    the shapes need the shader's clamping)."""
+    sa = [int(x) for x in shapes[0:ndim]]
+    sb = [int(x) for x in shapes[ndim:2 * ndim]]
+    sc = [int(x) for x in shapes[2 * ndim:3 * ndim]]
+    for s in (sa, sb):
+        if any(x not in (1, c) for x, c in zip(s, sc)):
+            return None
+    na, nb = int(np.prod(sa)), int(np.prod(sb))
+    if a.size < na or b.size < nb:
+        return None
+    return np.broadcast_to(a[:na].reshape(sa), sc), np.broadcast_to(b[:nb].reshape(sb), sc)
+
+
 def _bcast_index2(ai, shapes, sizes, ndim):
     """iadd_broadcast.comp:22-41 (index into b for every element of a)."""
     size = np.array(sizes, dtype=np.int64)
@@ -182,6 +199,10 @@ def _run(name: str, bufs, ds: DataShape, p):
         base = name[:-10]
         if base in _BIN:                       # Multi3BroadcastParams
             n = min(p.size2, ds.x)
+            views = _bcast_views(B[3], p.ndim, B[0], B[1]) if n == p.size2 else None
+            if views is not None:
+                B[2][:n] = _binop(_BIN[base], views[0], views[1]).reshape(-1)
+                return
             ci = np.arange(n)
             ab = _bcast_index3(ci, B[3], (p.size0, p.size1, p.size2), p.ndim)
             B[2][:n] = _binop(_BIN[base], B[0][ab[0]], B[1][ab[1]])
