@@ -254,6 +254,7 @@ def gpu_arm(args, rank, world, dist):
         extra["chain"] = chain_study(vk, gpu, timer)
         extra["reduction_precision"] = reduction_precision_study(vk, gpu, timer)
         extra["train_loop"] = train_loop_study(vk, gpu)
+        extra["small_suite"] = small_suite_study(vk, gpu, timer)
 
     result = {
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -577,6 +578,111 @@ def chain32(x, y):
     t = (t - y) * (t + y)
     t = t.tanh() + t.sign()
     return t * 0.5
+
+
+def small_suite_study(vk, gpu, timer, reps=100):
+    """The plain-fp32 small op suite (numpy seed 0, in this order): A (512,1024)
+    and B (1,1024) uniform[-1,1); M1, M2 (256,256) N(0,1); 4096 indices in
+    [0, 524288); Xoshiro128pp(size 64, seed 0) with 65536 uniforms and 65536
+    normals.  Latency-bound, so per op:
+      api_us     host wall time per call through the public API (calls back
+                 to back, one wait at the end: launch cost included);
+      device_us  device time per call, the calls captured in a CUDA graph and
+                 replayed (CUDA events), i.e. without host launch cost;
+      oracle_us  the oracle's C restatement of the shader on all host
+                 threads (the reference's own CPU path is unavailable);
+      numpy_us   numpy, where numpy has the op."""
+    import time as _time
+    from oracle import ops as O  # CPU baseline column only
+    L = O.lib()
+    rng = np.random.default_rng(0)
+    A_ = rng.uniform(-1, 1, size=(512, 1024)).astype(np.float32)
+    B_ = rng.uniform(-1, 1, size=(1, 1024)).astype(np.float32)
+    M1 = rng.standard_normal((256, 256)).astype(np.float32)
+    M2 = rng.standard_normal((256, 256)).astype(np.float32)
+    idx = rng.integers(0, 524288, 4096).astype(np.uint32)
+    a, b = vk.Array(gpu, data=A_), vk.Array(gpu, data=B_)
+    m1, m2 = vk.Array(gpu, data=M1), vk.Array(gpu, data=M2)
+    ix = vk.U32Array(gpu, data=idx)
+    r = vk.random.Xoshiro128pp(gpu, size=64, seed=0)
+    ops = {
+        "A+B": lambda: a + b, "A*B": lambda: a * b, "A/(|B|+1)": lambda: a / (b.abs() + 1.0),
+        "A**2": lambda: a ** 2.0, "exp(A)": lambda: a.exp(), "tanh(A)": lambda: a.tanh(),
+        "clamp(A,-.5,.5)": lambda: a.clamp(-0.5, 0.5),
+        "sum0": lambda: a.sum(axis=0), "sum1": lambda: a.sum(axis=1), "sum": lambda: a.sum(),
+        "mean0": lambda: a.mean(axis=0), "mean1": lambda: a.mean(axis=1), "mean": lambda: a.mean(),
+        "max0": lambda: a.maximum(axis=0), "max1": lambda: a.maximum(axis=1), "max": lambda: a.maximum(),
+        "M1@M2": lambda: m1 @ m2, "gather4096": lambda: a.gather(ix),
+        "random65536": lambda: r.random(shape=(65536,)), "normal65536": lambda: r.normal(shape=(65536,)),
+    }
+    p = lambda x: x.ctypes.data
+    sa, sb = np.array([512, 1024], np.int64), np.array([1, 1024], np.int64)
+    out = np.empty_like(A_)
+    r0, r1 = np.empty(1024, np.float32), np.empty(512, np.float32)
+    st = O.Xoshiro128pp(0, 64)
+    u = np.empty(65536, np.float32)
+    oracle = {
+        "A+B": lambda: L.bcast_binary(0, p(A_), p(sa), p(B_), p(sb), p(out), p(sa), 2),
+        "A*B": lambda: L.bcast_binary(2, p(A_), p(sa), p(B_), p(sb), p(out), p(sa), 2),
+        "exp(A)": lambda: L.ew_unary(14, p(A_), p(out), A_.size),
+        "tanh(A)": lambda: L.ew_unary(10, p(A_), p(out), A_.size),
+        "A**2": lambda: L.ew_scalar(4, p(A_), np.float32(2.0), p(out), A_.size),
+        "sum0": lambda: L.reduce_axis(0, p(A_), 1, 512, 1024, p(r0)),
+        "sum1": lambda: L.reduce_axis(0, p(A_), 512, 1024, 1, p(r1)),
+        "sum": lambda: L.reduce_all(0, p(A_), A_.size),
+        "max0": lambda: L.reduce_axis(2, p(A_), 1, 512, 1024, p(r0)),
+        "max1": lambda: L.reduce_axis(2, p(A_), 512, 1024, 1, p(r1)),
+        "M1@M2": lambda: O.matmul(M1, M2),
+        "gather4096": lambda: O.gather(A_.reshape(-1), idx),
+        "random65536": lambda: L.xo_generate(p(st.state), 64, p(u), 65536, 1),
+        "normal65536": lambda: st.normal(65536),
+    }
+    npy = {
+        "A+B": lambda: A_ + B_, "A*B": lambda: A_ * B_, "A/(|B|+1)": lambda: A_ / (np.abs(B_) + np.float32(1)),
+        "A**2": lambda: A_ * A_, "exp(A)": lambda: np.exp(A_), "tanh(A)": lambda: np.tanh(A_),
+        "clamp(A,-.5,.5)": lambda: np.clip(A_, -0.5, 0.5), "sum0": lambda: A_.sum(axis=0),
+        "sum1": lambda: A_.sum(axis=1), "sum": lambda: A_.sum(), "max0": lambda: A_.max(axis=0),
+        "max1": lambda: A_.max(axis=1), "max": lambda: A_.max(), "M1@M2": lambda: M1 @ M2,
+        "gather4096": lambda: A_.reshape(-1)[idx],
+    }
+
+    def host_us(fn, n):
+        fn()
+        t0 = _time.perf_counter()
+        for _ in range(n):
+            fn()
+        return (_time.perf_counter() - t0) / n * 1e6
+
+    res = {}
+    for name, fn in ops.items():
+        for _ in range(3):
+            fn()
+        gpu.wait()
+        t0 = _time.perf_counter()
+        keep = [fn() for _ in range(reps)]
+        gpu.wait()
+        api = (_time.perf_counter() - t0) / reps * 1e6
+        del keep
+        g = vk.graph.Graph(gpu)
+        with g:
+            keep = [fn() for _ in range(reps)]
+        g.launch()
+        gpu.wait()
+        t0 = timer.mark()
+        g.launch()
+        t1 = timer.mark()
+        gpu.wait()
+        dev = timer.ms(t0, t1) / reps * 1e3
+        timer.free(t0, t1)
+        del g, keep
+        row = {"api_us": round(api, 2), "device_us": round(dev, 2)}
+        if name in oracle:
+            row["oracle_us"] = round(host_us(oracle[name], 20), 1)
+        if name in npy:
+            row["numpy_us"] = round(host_us(npy[name], 20), 1)
+        res[name] = row
+    return {"ops": res, "reps": reps, "oracle_threads": int(L.oracle_threads()),
+            "note": "latency suite: parity with the reference is checked by tests/test_gpu_golden.py (small_suite_*)"}
 
 
 def train_loop_study(vk, gpu, epochs=100, batch=32):
