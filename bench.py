@@ -348,7 +348,7 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
 
 
 # ---------------------------------------------------------------- matmul / MLP
-def matmul_study(vk, gpu, timer, sizes=(4096, 8192)):
+def matmul_study(vk, gpu, timer, sizes=(4096, 8192), precisions=("fp32", "bf16", "bf16x3")):
     """C = A @ B, A, B ~ N(0,1) fp32 (seed 0), in fp32 SIMT, bf16 and split
     bf16x3 on tensor cores: TFLOP/s (2MNK / CUDA-event time) and relative
     Frobenius error vs float64 over the first 128 rows of C."""
@@ -359,7 +359,7 @@ def matmul_study(vk, gpu, timer, sizes=(4096, 8192)):
         B = rng.standard_normal((n, n), dtype=np.float32)
         ref = A[:128].astype(np.float64) @ B.astype(np.float64)
         a, b = vk.Array(gpu, data=A), vk.Array(gpu, data=B)
-        for prec in ("fp32", "bf16", "bf16x3"):
+        for prec in precisions:
             c = vk.vkarray.matmul(a, b, precision=prec)
             gpu.wait()
             reps = 3 if (prec == "fp32" and n >= 8192) else 10
@@ -377,12 +377,13 @@ def matmul_study(vk, gpu, timer, sizes=(4096, 8192)):
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak = json.load(open(peaks_path))["bf16_tflops"] if os.path.exists(peaks_path) else 1900.0
     best = out.get(f"bf16x3_{sizes[-1]}", {}).get("tflops")
+    base = out.get(f"fp32_{sizes[-1]}", {}).get("tflops")
     return {"unit": "TFLOP/s (2MNK)", "results": out, "bf16_peak_tflops": peak,
-            "bf16x3_vs_fp32_speedup": round(best / out[f"fp32_{sizes[-1]}"]["tflops"], 2) if best else None,
+            "bf16x3_vs_fp32_speedup": round(best / base, 2) if best and base else None,
             "note": "bf16x3 issues 3 tensor products per K step; TFLOP/s counts the algorithmic 2MNK"}
 
 
-def mlp_study(vk, gpu, timer, steps=50):
+def mlp_study(vk, gpu, timer, steps=50, precisions=("fp32", "bf16x3")):
     """One Sequence.train step of Dense 784-1024, ReLU, Dense 1024-1024,
     Sigmoid, Dense 1024-10, softmax cross entropy, Adam(1e-3), batch 256,
     HeNormal(seed 1); steps/s for fp32 SIMT vs split-bf16x3 matmuls."""
@@ -391,7 +392,7 @@ def mlp_study(vk, gpu, timer, steps=50):
     X = rng.standard_normal((256, 784)).astype(np.float32)
     Y = np.eye(10, dtype=np.float32)[rng.integers(0, 10, 256)]
     res = {}
-    for prec in ("fp32", "bf16x3"):
+    for prec in precisions:
         gpu.matmul_precision = prec
         opt = nn.Adam(gpu, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8)
         net = nn.Sequence([
@@ -432,10 +433,11 @@ def mlp_study(vk, gpu, timer, steps=50):
     gpu.matmul_precision = "fp32"
     flop = 3 * 2 * 256 * (784 * 1024 + 1024 * 1024 + 1024 * 10)
     res["flop_per_step"] = flop
-    res["speedup_bf16x3_graph_vs_fp32_eager"] = round(res["bf16x3_graph"]["steps_per_s"] /
-                                                      res["fp32"]["steps_per_s"], 2)
-    res["speedup_bf16x3_graph_vs_fp32_graph"] = round(res["bf16x3_graph"]["steps_per_s"] /
-                                                      res["fp32_graph"]["steps_per_s"], 2)
+    if "fp32" in res and "bf16x3" in res:
+        res["speedup_bf16x3_graph_vs_fp32_eager"] = round(res["bf16x3_graph"]["steps_per_s"] /
+                                                          res["fp32"]["steps_per_s"], 2)
+        res["speedup_bf16x3_graph_vs_fp32_graph"] = round(res["bf16x3_graph"]["steps_per_s"] /
+                                                          res["fp32_graph"]["steps_per_s"], 2)
     return res
 
 
@@ -920,6 +922,22 @@ def reference_arm(args, rank, world):
             "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_study(args):
+    import vulkpy_gb300 as vk
+    gpu = vk.GPU(0)
+    timer = Timer(vk, gpu)
+    if args.study == "matmul":
+        return matmul_study(vk, gpu, timer, sizes=tuple(int(x) for x in args.mm_sizes.split(",")),
+                            precisions=tuple(args.mm_precisions.split(",")))
+    if args.study == "mlp":
+        return mlp_study(vk, gpu, timer, precisions=tuple(args.mm_precisions.split(",")))
+    fn = {"batched": batched_study, "chain": chain_study,
+          "reduction_precision": reduction_precision_study, "small_suite": small_suite_study}.get(args.study)
+    if fn is None:
+        return train_loop_study(vk, gpu)
+    return fn(vk, gpu, timer)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -935,7 +953,15 @@ def main():
     ap.add_argument("--cpu-passes", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the matmul and MLP studies")
+    ap.add_argument("--study", default=None,
+                    choices=["matmul", "mlp", "batched", "chain", "reduction_precision", "train_loop", "small_suite"],
+                    help="run only this study (a small case for profiling) and print its JSON")
+    ap.add_argument("--mm-sizes", default="4096,8192", help="matmul study sizes, comma separated")
+    ap.add_argument("--mm-precisions", default="fp32,bf16,bf16x3", help="matmul study precisions")
     args = ap.parse_args()
+    if args.study is not None:
+        print(json.dumps(run_study(args)), flush=True)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -1,5 +1,5 @@
 """
-Split-K autotuner for the split-bf16x3 tensor-core GEMM.
+Split-K autotuner for the tensor-core GEMM (bf16 and split-bf16x3).
 
 For each size bucket (ceil(log2) of M, N and K) the tuner times every
 candidate split count on a representative problem of that bucket and keeps
@@ -43,10 +43,11 @@ def load_table(path: str = TABLE_PATH) -> int:
     with open(path) as f:
         data = json.load(f)
     n = 0
-    for m, nn, k, splits in data.get("bf16x3", []):
-        # representative sizes: the top of each bucket
-        check(lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 1 << m, 1 << nn, 1 << k, int(splits)))
-        n += 1
+    for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16)):
+        for m, nn, k, splits in data.get(name, []):
+            # representative sizes: the top of each bucket
+            check(lib.vkc_gemm_tune_set(prec, 1 << m, 1 << nn, 1 << k, int(splits)))
+            n += 1
     return n
 
 
@@ -75,15 +76,16 @@ def default_shapes() -> List[Tuple[int, int, int]]:
     return sorted(rep.values())
 
 
-def _time_gemm(gpu, a, b, c, m, n, k, reps=5, calls=16) -> float:
+def _time_gemm(gpu, a, b, c, m, n, k, reps=5, calls=16, prec=None) -> float:
     """Device time of one call in ms.  The calls are captured in a CUDA
     graph and replayed, so host-side launch cost (which a graph removes)
     does not decide the choice."""
     lib_ = lib
     h = gpu.handle
+    prec = _lib.MM_BF16X3 if prec is None else prec
 
     def run():
-        check(lib_.vkc_gemm(h, _lib.MM_BF16X3, 0, 1, m, n, k, C.c_float(1.0), a, k, b, k, C.c_float(0.0), c, n))
+        check(lib_.vkc_gemm(h, prec, 0, 1, m, n, k, C.c_float(1.0), a, k, b, k, C.c_float(0.0), c, n))
 
     run()
     check(lib_.vkc_device_synchronize(h))
@@ -119,30 +121,33 @@ def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) ->
     gpu = vk.GPU()
     shapes = list(shapes or default_shapes())
     check(lib.vkc_gemm_tune_clear())
-    entries = []
-    for (m, n, k) in shapes:
-        rng = np.random.default_rng(m * 31 + n * 7 + k)
-        A = vk.Array(gpu, data=rng.standard_normal((m, k)).astype(np.float32))
-        B = vk.Array(gpu, data=rng.standard_normal((n, k)).astype(np.float32))
-        Cm = vk.Array(gpu, shape=(m, n))
-        nk = (k + 63) // 64
-        best, best_ms = 1, float("inf")
-        results = {}
-        for s in CANDIDATES:
-            if s > max(1, nk):
-                continue
-            check(lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, s))
-            ms = _time_gemm(gpu, A._dptr(), B._dptr(), Cm._buf.ptr, m, n, k)
-            results[s] = round(ms * 1e3, 1)
-            if ms < best_ms:
-                best, best_ms = s, ms
-        check(lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, best))
-        entries.append([bucket(m), bucket(n), bucket(k), best])
-        if verbose:
-            print(f"M={m} N={n} K={k}: best splits {best} ({best_ms * 1e3:.1f} us)  {results}", flush=True)
-    table = {"bf16x3": entries, "device": vk.GPU()._dev.name,
-             "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
-             "candidates": list(CANDIDATES)}
+    table = {}
+    for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16)):
+        entries = []
+        for (m, n, k) in shapes:
+            rng = np.random.default_rng(m * 31 + n * 7 + k)
+            A = vk.Array(gpu, data=rng.standard_normal((m, k)).astype(np.float32))
+            B = vk.Array(gpu, data=rng.standard_normal((n, k)).astype(np.float32))
+            Cm = vk.Array(gpu, shape=(m, n))
+            nk = (k + 63) // 64
+            best, best_ms = 1, float("inf")
+            results = {}
+            for s in CANDIDATES:
+                if s > max(1, nk):
+                    continue
+                check(lib.vkc_gemm_tune_set(prec, m, n, k, s))
+                ms = _time_gemm(gpu, A._dptr(), B._dptr(), Cm._buf.ptr, m, n, k, prec=prec)
+                results[s] = round(ms * 1e3, 1)
+                if ms < best_ms:
+                    best, best_ms = s, ms
+            check(lib.vkc_gemm_tune_set(prec, m, n, k, best))
+            entries.append([bucket(m), bucket(n), bucket(k), best])
+            if verbose:
+                print(f"{name} M={m} N={n} K={k}: best splits {best} ({best_ms * 1e3:.1f} us)  {results}",
+                      flush=True)
+        table[name] = entries
+    table.update({"device": vk.GPU()._dev.name, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
+                  "candidates": list(CANDIDATES)})
     return table
 
 
@@ -151,7 +156,7 @@ def main():
     out = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else TABLE_PATH
     with open(out, "w") as f:
         json.dump(table, f, indent=1)
-    print(f"wrote {len(table['bf16x3'])} entries to {out}")
+    print(f"wrote {len(table['bf16x3'])} + {len(table['bf16'])} entries to {out}")
 
 
 if __name__ == "__main__":

@@ -8,12 +8,11 @@
 // keeps ~16 significant bits per operand (relative representation error
 // <= 2^-17) at three tensor-core products instead of fp32 FMA.
 //
-// One CTA computes a 128 x BN tile with 6 warps:
-//   warp 0 lane 0  TMA producer: STAGES-deep ring of (A, B[, A_lo, B_lo]) tiles
-//   warp 1         allocates TMEM; lane 0 issues tcgen05.mma and commits
-//   warps 2-5      epilogue: tcgen05.ld 32 columns at a time, alpha/beta/bias/act
-// Every mbarrier wait is bounded by a wall-clock limit; on expiry the CTA
-// records bit1 in the device error word, drains what it issued and returns.
+// k_gemm_tcp is persistent (one CTA per SM, 2-CTA clusters sharing the op(B)
+// tile through TMA multicast) with two TMEM accumulators, so a tile's
+// epilogue overlaps the next tile's MMAs.  Every mbarrier wait is bounded by
+// a wall-clock limit; on expiry the CTA records bit1 in the device error
+// word, drains what it issued and returns.
 #include "gemm_tc.cuh"
 #include "tc_ptx.cuh"
 
@@ -29,203 +28,142 @@ namespace vkc {
 namespace {
 
 // ------------------------------------------------------------ the kernel
-template <int BN, bool X3, int STAGES>
-struct TcCfg {
-  static constexpr uint32_t kABytes = kBM * kBK * 2;
-  static constexpr uint32_t kBBytes = BN * kBK * 2;
+// Persistent, cluster-paired tensor-core GEMM.
+//
+// Work unit: a 256 x 256 block of C (two 128-row tiles, one per CTA of a
+// 2-CTA cluster) over one K range (split K).  The two CTAs of a cluster walk
+// the same unit sequence in lockstep; each loads its own 128 rows of op(A)
+// and one 128-row half of the shared op(B) tile, multicast to both CTAs, so
+// every CTA reads 32 KB (bf16) or 64 KB (split) from L2 per 64-wide K block
+// instead of 48 / 96 KB.  Each CTA computes its 128 x 256 tile with
+// single-CTA tcgen05.mma (M=128, N=256, K=16) into one of two 256-column TMEM
+// accumulators, so the epilogue of one accumulation overlaps the MMAs of the
+// next.
+//
+// Warps: 0 = TMA producer (lane 0), 1 = TMEM owner + MMA issuer (lane 0),
+// 2..9 = epilogue.  Epilogue warp w reads TMEM lanes 32*(w%4).. (the lane
+// quarter its warp rank allows) and columns 128*((w-2)/4).. of a buffer.
+//
+// bf16 mode: one accumulation per unit over the whole K range.
+// split mode (hi*hi + hi*lo + lo*hi): one accumulation per DRAIN K blocks;
+// the epilogue adds each into fp32 registers with round-to-nearest, so the
+// tensor pipe's truncating accumulation spans at most DRAIN*64 of K.
+constexpr int kBN2 = 256;          // columns of C per CTA tile
+constexpr int kEpiWarps = 8;
+constexpr int kThreadsP = 32 * (2 + kEpiWarps);
+constexpr int kGroupM = 8;         // cluster rows per raster group (L2 reuse)
+
+
+template <bool X3, int STAGES>
+struct PCfg {
+  static constexpr uint32_t kABytes = kBM * kBK * 2;             // 16 KB
+  static constexpr uint32_t kBHalf = 128 * kBK * 2;              // 16 KB
+  static constexpr uint32_t kBBytes = kBN2 * kBK * 2;            // 32 KB
   static constexpr uint32_t kStageBytes = (X3 ? 2u : 1u) * (kABytes + kBBytes);
-  static constexpr uint32_t kSmem = STAGES * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
-  static constexpr uint32_t kTmemCols = BN;  // fp32 accumulator: one column per output column
+  static constexpr uint32_t kBarOff = STAGES * kStageBytes;
+  // full[S], empty[S], accf[2], acce[2], drain, then tmem slot + abort flag
+  static constexpr uint32_t kSlotOff = kBarOff + 8u * (2 * STAGES + 5);
+  static constexpr uint32_t kSmem = kSlotOff + 16 + 1024 /*alignment slack*/;
 };
 
-template <int BN, bool X3, int STAGES>
-__global__ void __launch_bounds__(kThreadsTC, 1)
-k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-          const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N, int K,
-          float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-          uint32_t* err) {
-  using Cfg = TcCfg<BN, X3, STAGES>;
-  extern __shared__ uint8_t smem_raw[];
-  const uint32_t raw = smem_u32(smem_raw);
-  const uint32_t base = (raw + 1023u) & ~1023u;
-  uint8_t* gbase = smem_raw + (base - raw);
-  const uint32_t bars = base + STAGES * Cfg::kStageBytes;
-  auto full_bar = [&](int s) { return bars + 8u * s; };
-  auto empty_bar = [&](int s) { return bars + 8u * (STAGES + s); };
-  const uint32_t acc_bar = bars + 16u * STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * Cfg::kStageBytes + 16 * STAGES + 8);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+struct PUnit {
+  int m0, n0, kb0, nkb, z;
+};
 
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
-  const int nk = (K + kBK - 1) / kBK;
+__device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int m_pairs, int n_blocks, int rank) {
+  const int tile = u / splits, z = u - tile * splits;
+  const int per_group = kGroupM * n_blocks;
+  const int g = tile / per_group, first = g * kGroupM;
+  const int gsize = min(kGroupM, m_pairs - first);
+  const int within = tile - g * per_group;
+  const int mp = first + within % gsize, nb = within / gsize;
+  PUnit p;
+  p.m0 = (2 * mp + rank) * kBM;
+  p.n0 = nb * kBN2;
+  p.kb0 = z * kps;
+  p.nkb = max(0, min(nk, p.kb0 + kps) - p.kb0);
+  p.z = z;
+  return p;
+}
 
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
-      mbar_init(full_bar(s), 1);
-      mbar_init(empty_bar(s), 1);
-    }
-    mbar_init(acc_bar, 1);
-    *abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(Cfg::kTmemCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
-
-  auto stage_a = [&](int s) { return base + s * Cfg::kStageBytes; };
-  auto stage_b = [&](int s) { return stage_a(s) + Cfg::kABytes; };
-  auto stage_alo = [&](int s) { return stage_b(s) + Cfg::kBBytes; };
-  auto stage_blo = [&](int s) { return stage_alo(s) + Cfg::kABytes; };
-
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    int issued = 0;
-    bool ok = true;
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (kb / STAGES) & 1;
-      if (*abort_flag || !mbar_wait(empty_bar(s), ph ^ 1)) { ok = false; break; }
-      mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
-      tma_load_2d(stage_a(s), &map_a, full_bar(s), kb * kBK, m0);
-      tma_load_2d(stage_b(s), &map_b, full_bar(s), kb * kBK, n0);
-      if (X3) {
-        tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kb * kBK, m0);
-        tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kb * kBK, n0);
-      }
-      ++issued;
-    }
-    if (!ok) {
-      atomicOr(err, 2u);
-      *abort_flag = 1;
-      // drain the copies still in flight into this CTA's shared memory
-      for (int kb = std::max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1);
-    }
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer
-    constexpr uint32_t idesc = (1u << 4)            // D: fp32
-                               | (1u << 7)          // A: bf16
-                               | (1u << 10)         // B: bf16
-                               | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
-    bool ok = true;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (kb / STAGES) & 1;
-      if (*abort_flag || !mbar_wait(full_bar(s), ph)) { ok = false; break; }
-      tc_fence_after();
+// v = act(alpha * acc + beta * c + bias) for 32 consecutive columns of one row.
+__device__ __forceinline__ void store_row32(const float* acc, float* crow, const float* bias, int col0, int N,
+                                            float alpha, float beta, int act, bool raw) {
+  const bool vec = ((reinterpret_cast<uintptr_t>(crow + col0) & 15u) == 0) && (col0 + 32 <= N);
+  if (vec) {
 #pragma unroll
-      for (int k = 0; k < kBK / 16; ++k) {
-        const uint64_t a = sw128_desc(stage_a(s) + 32u * k);
-        const uint64_t b = sw128_desc(stage_b(s) + 32u * k);
-        mma_bf16(tmem, a, b, idesc, (kb | k) != 0);
-        if (X3) {
-          mma_bf16(tmem, a, sw128_desc(stage_blo(s) + 32u * k), idesc, 1);
-          mma_bf16(tmem, sw128_desc(stage_alo(s) + 32u * k), b, idesc, 1);
+    for (int j = 0; j < 32; j += 4) {
+      float4 v = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
+      if (!raw) {
+        float* pv = &v.x;
+        float4 old = beta != 0.f ? *reinterpret_cast<const float4*>(crow + col0 + j) : make_float4(0, 0, 0, 0);
+        const float* po = &old.x;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          float x = alpha * pv[t];
+          if (beta != 0.f) x += beta * po[t];
+          if (bias) x += bias[col0 + j + t];
+          if (act == VKC_ACT_RELU) x = fmaxf(x, 0.f);
+          else if (act == VKC_ACT_SIGMOID) x = 1.0f / (1.0f + expf(0.0f - x));
+          pv[t] = x;
         }
       }
-      mma_commit(empty_bar(s));  // frees the stage once these MMAs have read it
+      *reinterpret_cast<float4*>(crow + col0 + j) = v;
     }
-    if (!ok) {
-      atomicOr(err, 2u);
-      *abort_flag = 1;
-    }
-    mma_commit(acc_bar);  // fires when every MMA issued above has completed
-  } else if (warp >= 2) {
-    // ---------------- epilogue: TMEM -> registers -> global
-    const bool ok = mbar_wait(acc_bar, 0) && !*abort_flag && nk > 0;
-    tc_fence_after();
-    const int q = warp & 3;  // TMEM lanes 32q .. 32q+31 belong to this warp
-    const int row = m0 + q * 32 + lane;
-    if (!ok) {
-      if (lane == 0) atomicOr(err, 2u);
-    } else {
-#pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), r);
-        if (row < M) {
-          float* crow = C + (int64_t)row * ldc;
+  } else {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int col = n0 + c * 32 + j;
-            if (col < N) {
-              float v = alpha * __uint_as_float(r[j]);
-              if (beta != 0.f) v += beta * crow[col];
-              if (bias) v += bias[col];
-              if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
-              else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-              crow[col] = v;
-            }
-          }
+    for (int j = 0; j < 32; ++j) {
+      const int col = col0 + j;
+      if (col < N) {
+        float x = acc[j];
+        if (!raw) {
+          x = alpha * x;
+          if (beta != 0.f) x += beta * crow[col];
+          if (bias) x += bias[col];
+          if (act == VKC_ACT_RELU) x = fmaxf(x, 0.f);
+          else if (act == VKC_ACT_SIGMOID) x = 1.0f / (1.0f + expf(0.0f - x));
         }
+        crow[col] = x;
       }
     }
-  }
-
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 1) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols) : "memory");
   }
 }
 
-// ------------------------------------------------------------ split-bf16x3
-// The tensor core adds each MMA's result into the fp32 TMEM accumulator
-// with truncation, so the error of one long accumulation grows with K/16
-// (measured: 1.5e-5 relative at K = 4096, 2.9e-5 at 8192).  This kernel
-// restarts the accumulation every 64-wide K block in one of kAccBufs TMEM
-// buffers and the epilogue warps add each block's partial into fp32
-// registers with round-to-nearest, overlapping with the next blocks' MMAs.
-
-// With gridDim.z > 1 the K blocks are split across CTAs (blockIdx.z takes
-// blocks [z*kps, (z+1)*kps)) and each CTA writes its raw fp32 partial tile to
-// partial[z][M][N]; k_splitk_reduce then adds the partials in z order and
-// applies the epilogue, so results do not depend on scheduling.
-template <int STAGES>
-__global__ void __launch_bounds__(kThreadsTC, 1)
-k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-             const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
-             int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-             uint32_t* err, float* __restrict__ partial, int kps) {
-  constexpr int BN = 128;
-  using Cfg = TcCfg<BN, true, STAGES>;
-  constexpr uint32_t kCols = BN * kAccBufs;  // 512: all of TMEM
+template <bool X3, int STAGES, int DRAIN>
+__global__ void __launch_bounds__(kThreadsP, 1)
+k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+           const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
+           int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
+           uint32_t* err, float* __restrict__ partial, int splits, int kps, int m_pairs, int n_blocks) {
+  using Cfg = PCfg<X3, STAGES>;
+  constexpr uint32_t kCols = 2 * kBN2;  // two accumulators: all 512 TMEM columns
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t* gbase = smem_raw + (base - raw);
-  const uint32_t bars = base + STAGES * Cfg::kStageBytes;
+  const uint32_t bars = base + Cfg::kBarOff;
   auto full_bar = [&](int s) { return bars + 8u * s; };
   auto empty_bar = [&](int s) { return bars + 8u * (STAGES + s); };
   auto accf_bar = [&](int b) { return bars + 8u * (2 * STAGES + b); };
-  auto acce_bar = [&](int b) { return bars + 8u * (2 * STAGES + kAccBufs + b); };
-  const uint32_t drain_bar = bars + 8u * (2 * STAGES + 2 * kAccBufs);
-  uint32_t* tmem_slot =
-      reinterpret_cast<uint32_t*>(gbase + STAGES * Cfg::kStageBytes + 8 * (2 * STAGES + 2 * kAccBufs + 1));
+  auto acce_bar = [&](int b) { return bars + 8u * (2 * STAGES + 2 + b); };
+  const uint32_t drain_bar = bars + 8u * (2 * STAGES + 4);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + Cfg::kSlotOff);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * BN;
-  const int nk_all = (K + kBK - 1) / kBK;
-  const int kb0 = blockIdx.z * kps;
-  const int nk = max(0, min(nk_all, kb0 + kps) - kb0);  // K blocks of this CTA
+  const int rank = (int)cluster_ctarank();
+  const int cluster = blockIdx.x >> 1, nclusters = gridDim.x >> 1;
+  const int nk = (K + kBK - 1) / kBK;
+  const int units = m_pairs * n_blocks * splits;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(full_bar(s), 1);
-      mbar_init(empty_bar(s), 1);
+      mbar_init(empty_bar(s), 2);  // one commit from each CTA's MMA issuer
     }
-    for (int b = 0; b < kAccBufs; ++b) {
+    for (int b = 0; b < 2; ++b) {
       mbar_init(accf_bar(b), 1);
-      mbar_init(acce_bar(b), 4);  // one arrive per epilogue warp
+      mbar_init(acce_bar(b), kEpiWarps);
     }
     mbar_init(drain_bar, 1);
     *abort_flag = 0;
@@ -238,7 +176,9 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
-  __syncthreads();
+  // the peer multicasts into this CTA's stages and barriers: both CTAs'
+  // barriers must be initialised before either producer starts
+  cluster_sync_all();
   tc_fence_after();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
 
@@ -248,70 +188,143 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
   auto stage_blo = [&](int s) { return stage_alo(s) + Cfg::kABytes; };
 
   if (warp == 0 && lane == 0) {
-    int issued = 0;
+    // ---------------- TMA producer
+    int it = 0;
     bool ok = true;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      if (*abort_flag || !mbar_wait(empty_bar(s), ((kb / STAGES) & 1) ^ 1)) { ok = false; break; }
-      mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
-      const int kx = (kb0 + kb) * kBK;
-      tma_load_2d(stage_a(s), &map_a, full_bar(s), kx, m0);
-      tma_load_2d(stage_b(s), &map_b, full_bar(s), kx, n0);
-      tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kx, m0);
-      tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kx, n0);
-      ++issued;
+    for (int u = cluster; u < units && ok; u += nclusters) {
+      const PUnit p = unit_of(u, splits, kps, nk, m_pairs, n_blocks, rank);
+      const int nb_row = p.n0 + 128 * rank;
+      for (int kb = 0; kb < p.nkb; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (*abort_flag || !mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1)) { ok = false; break; }
+        mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
+        const int kx = (p.kb0 + kb) * kBK;
+        tma_load_2d(stage_a(s), &map_a, full_bar(s), kx, p.m0);
+        tma_load_2d_mc(stage_b(s) + rank * Cfg::kBHalf, &map_b, full_bar(s), kx, nb_row, 3);
+        if (X3) {
+          tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kx, p.m0);
+          tma_load_2d_mc(stage_blo(s) + rank * Cfg::kBHalf, &map_blo, full_bar(s), kx, nb_row, 3);
+        }
+      }
     }
     if (!ok) {
       atomicOr(err, 2u);
       *abort_flag = 1;
-      for (int kb = std::max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full_bar(kb % STAGES), (kb / STAGES) & 1);
     }
-  } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                               ((uint32_t)(kBM >> 4) << 24);
-    bool ok = true;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES, b = kb % kAccBufs;
-      if (*abort_flag || !mbar_wait(full_bar(s), (kb / STAGES) & 1) ||
-          !mbar_wait(acce_bar(b), ((kb / kAccBufs) & 1) ^ 1)) {
-        ok = false;
+    // Tail: wait until both CTAs' MMAs have released every stage, so no
+    // commit from the peer is still in flight towards this CTA at exit.
+    for (int t = 0; t < STAGES && it - STAGES + t >= 0; ++t) {
+      const int j = it - STAGES + t;
+      if (!mbar_wait(empty_bar(j % STAGES), (j / STAGES) & 1)) {
+        atomicOr(err, 2u);
         break;
       }
-      tc_fence_after();
-      const uint32_t d = tmem + (uint32_t)(b * BN);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    constexpr uint32_t idesc = (1u << 4)            // D: fp32
+                               | (1u << 7)          // A: bf16
+                               | (1u << 10)         // B: bf16
+                               | ((uint32_t)(kBN2 >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+    int it = 0, acc_it = 0;
+    bool ok = true;
+    for (int u = cluster; u < units && ok; u += nclusters) {
+      const PUnit p = unit_of(u, splits, kps, nk, m_pairs, n_blocks, rank);
+      const int span = X3 ? DRAIN : p.nkb;  // K blocks per accumulation
+      for (int g0 = 0; g0 < p.nkb && ok; g0 += span, ++acc_it) {
+        const int b = acc_it & 1;
+        if (*abort_flag || !mbar_wait(acce_bar(b), ((acc_it >> 1) & 1) ^ 1)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(b * kBN2);
+        const int g1 = min(p.nkb, g0 + span);
+        for (int kb = g0; kb < g1; ++kb, ++it) {
+          const int s = it % STAGES;
+          if (*abort_flag || !mbar_wait(full_bar(s), (it / STAGES) & 1)) { ok = false; break; }
+          tc_fence_after();
 #pragma unroll
-      for (int k = 0; k < kBK / 16; ++k) {
-        const uint64_t a = sw128_desc(stage_a(s) + 32u * k);
-        const uint64_t bb = sw128_desc(stage_b(s) + 32u * k);
-        // small cross terms first, the dominant hi*hi term last
-        mma_bf16(d, a, sw128_desc(stage_blo(s) + 32u * k), idesc, k != 0);
-        mma_bf16(d, sw128_desc(stage_alo(s) + 32u * k), bb, idesc, 1);
-        mma_bf16(d, a, bb, idesc, 1);
+          for (int k = 0; k < kBK / 16; ++k) {
+            const uint64_t a = sw128_desc(stage_a(s) + 32u * k);
+            const uint64_t bb = sw128_desc(stage_b(s) + 32u * k);
+            const uint32_t first = (kb == g0 && k == 0) ? 0u : 1u;
+            if (X3) {
+              // small cross terms first, the dominant hi*hi term last
+              mma_bf16(d, a, sw128_desc(stage_blo(s) + 32u * k), idesc, first);
+              mma_bf16(d, sw128_desc(stage_alo(s) + 32u * k), bb, idesc, 1);
+              mma_bf16(d, a, bb, idesc, 1);
+            } else {
+              mma_bf16(d, a, bb, idesc, first);
+            }
+          }
+          mma_commit_mc(empty_bar(s), 3);  // frees stage s in both CTAs once read
+        }
+        if (!ok) break;
+        mma_commit(accf_bar(b));
       }
-      mma_commit(empty_bar(s));
-      mma_commit(accf_bar(b));
     }
     if (!ok) {
       atomicOr(err, 2u);
       *abort_flag = 1;
     }
   } else if (warp >= 2) {
-    const int q = warp & 3;
-    const int row = m0 + q * 32 + lane;
-    float sum[BN];
+    // ---------------- epilogue: TMEM -> fp32 registers -> global
+    // The store loop runs over 32-column chunks read back from TMEM (not
+    // unrolled), so the alpha/beta/bias/activation code exists once: with a
+    // fully unrolled 128-column epilogue the kernel spent most of a small
+    // launch waiting on instruction fetch.
+    const int q = warp & 3;          // TMEM lane quarter
+    const int h = (warp - 2) >> 2;   // column half of the 256-wide tile
+    const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+    int acc_it = 0;
+    bool ok = true;
+    for (int u = cluster; u < units && ok; u += nclusters) {
+      const PUnit p = unit_of(u, splits, kps, nk, m_pairs, n_blocks, rank);
+      const int span = X3 ? DRAIN : p.nkb;
+      const int ngroups = (p.nkb + span - 1) / span;
+      float acc[X3 ? 128 : 1];
+      if (X3) {
 #pragma unroll
-    for (int j = 0; j < BN; ++j) sum[j] = 0.f;
-    bool ok = nk > 0;
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      const int b = kb % kAccBufs;
-      if (*abort_flag || !mbar_wait(accf_bar(b), (kb / kAccBufs) & 1)) { ok = false; break; }
-      tc_fence_after();
+        for (int j = 0; j < (X3 ? 128 : 1); ++j) acc[j] = 0.f;
+      }
+      int b = 0;
+      for (int gi = 0; gi < ngroups; ++gi, ++acc_it) {
+        b = acc_it & 1;
+        if (*abort_flag || !mbar_wait(accf_bar(b), (acc_it >> 1) & 1)) { ok = false; break; }
+        tc_fence_after();
+        if (X3) {
+          // add this accumulation to the fp32 sums; after the last one, put
+          // the sums back into the buffer for the store loop below
+          const bool last = gi == ngroups - 1;
 #pragma unroll
-      for (int c = 0; c < BN / 32; ++c) {
+          for (int c = 0; c < 4; ++c) {
+            const uint32_t ta = tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32);
+            uint32_t r[32];
+            tmem_ld32(ta, r);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              acc[(X3 ? c * 32 + j : 0)] += __uint_as_float(r[j]);
+              r[j] = __float_as_uint(acc[(X3 ? c * 32 + j : 0)]);
+            }
+            if (last) tmem_st32(ta, r);
+          }
+        }
+        if (gi + 1 < ngroups) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(acce_bar(b));
+        }
+      }
+      if (!ok) break;
+      if (ngroups == 0) continue;
+      const int row = p.m0 + q * 32 + lane;
+      const bool raw_out = partial != nullptr;
+      float* crow = raw_out ? partial + ((int64_t)p.z * M + row) * N : C + (int64_t)row * ldc;
+#pragma unroll 1
+      for (int c = 0; c < 4; ++c) {
         uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c * 32), r);
-#pragma unroll
-        for (int j = 0; j < 32; ++j) sum[c * 32 + j] += __uint_as_float(r[j]);
+        tmem_ld32(tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32), r);
+        const int col0 = p.n0 + h * 128 + c * 32;
+        if (row < M && col0 < N)
+          store_row32(reinterpret_cast<const float*>(r), crow, bias, col0, N, alpha, beta, act, raw_out);
       }
       tc_fence_before();
       __syncwarp();
@@ -320,48 +333,12 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
     if (!ok) {
       if (lane == 0) atomicOr(err, 2u);
       *abort_flag = 1;
-    } else {
-      // All MMAs are done, so the operand stages are free: stage this warp's
-      // 32 x 128 block in shared memory (row pitch 129 floats: conflict-free
-      // both ways) and write it back one coalesced 128-float row at a time.
-      float* tile = reinterpret_cast<float*>(gbase) + q * 32 * (BN + 1);
-#pragma unroll
-      for (int j = 0; j < BN; ++j) tile[lane * (BN + 1) + j] = sum[j];
-      __syncwarp();
-      for (int rr = 0; rr < 32; ++rr) {
-        const int grow = m0 + q * 32 + rr;
-        if (grow >= M) break;
-        if (partial) {  // split K: raw partial sums, epilogue after the reduction
-          float* prow = partial + ((int64_t)blockIdx.z * M + grow) * N;
-#pragma unroll
-          for (int i = 0; i < BN / 32; ++i) {
-            const int j = i * 32 + lane;
-            if (n0 + j < N) prow[n0 + j] = tile[rr * (BN + 1) + j];
-          }
-          continue;
-        }
-        float* crow = C + (int64_t)grow * ldc;
-#pragma unroll
-        for (int i = 0; i < BN / 32; ++i) {
-          const int j = i * 32 + lane;
-          const int col = n0 + j;
-          if (col < N) {
-            float v = alpha * tile[rr * (BN + 1) + j];
-            if (beta != 0.f) v += beta * crow[col];
-            if (bias) v += bias[col];
-            if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
-            else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-            crow[col] = v;
-          }
-        }
-      }
-      (void)row;
     }
   }
 
-  // Before TMEM is released every MMA must have completed.  On the normal
-  // path the epilogue waited for the last block's commit; after an abort the
-  // issuer commits once more and waits (bounded) for that.
+  // Before TMEM is released every MMA must have completed: on the normal
+  // path the epilogue waited for every accumulation's commit; after an abort
+  // the issuer commits once more and waits (bounded) for that.
   if (warp == 1 && lane == 0 && *abort_flag) {
     mma_commit(drain_bar);
     mbar_wait(drain_bar, 0);
@@ -372,9 +349,16 @@ k_gemm_tc_x3(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ 
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
   }
+  // neither CTA leaves while the other may still signal or fill its memory
+  cluster_sync_all();
 }
 
 // ------------------------------------------------------------ operand split
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& h, __nv_bfloat16& l) {
+  h = __float2bfloat16_rn(x);
+  l = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
 // K contiguous in the source: dst[r*Kp + k] from src[r*ld + k]; zero padding k >= K.
 __global__ void k_split_kmajor(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
                                __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
@@ -383,16 +367,92 @@ __global__ void k_split_kmajor(const float* __restrict__ src, int64_t R, int64_t
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
     const int64_t r = i / Kp, k = i - r * Kp;
     const float x = k < K ? src[r * ld + k] : 0.f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    __nv_bfloat16 h, l;
+    split_bf16(x, h, l);
     hi[i] = h;
-    if (lo) lo[i] = __float2bfloat16_rn(x - __bfloat162float(h));
+    if (lo) lo[i] = l;
   }
 }
 
-// K is the row index of the source (src[k*ld + r]): 32x32 tiles through
-// shared memory so both the read and the write are coalesced.
-__global__ void k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
-                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+// The same with 8 elements per thread: 2 x float4 in, one 16-byte store per
+// output (ld % 4 == 0, 16-byte aligned source, Kp % 8 == 0); the chunk that
+// straddles K is read element by element, chunks past K are zero.
+__global__ void __launch_bounds__(256)
+k_split_kmajor8(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
+                __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+  const int64_t per_row = Kp / 8, total = R * per_row;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const int64_t r = i / per_row, k = (i - r * per_row) * 8;
+    float x[8];
+    if (k + 8 <= K) {
+      const float4* p = reinterpret_cast<const float4*>(src + r * ld + k);
+      const float4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+      x[0] = v0.x, x[1] = v0.y, x[2] = v0.z, x[3] = v0.w, x[4] = v1.x, x[5] = v1.y, x[6] = v1.z, x[7] = v1.w;
+    } else {
+#pragma unroll
+      for (int t = 0; t < 8; ++t) x[t] = k + t < K ? src[r * ld + k + t] : 0.f;
+    }
+    __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) split_bf16(x[t], h[t], l[t]);
+    *reinterpret_cast<uint4*>(hi + r * Kp + k) = *reinterpret_cast<const uint4*>(h);
+    if (lo) *reinterpret_cast<uint4*>(lo + r * Kp + k) = *reinterpret_cast<const uint4*>(l);
+  }
+}
+
+// K is the row index of the source (src[k*ld + r]): 64 (k) x 64 (r) tiles
+// through shared memory.  Reads: each thread one float4 of a k row (16 rows
+// of 256 bytes per pass); writes: each thread 8 consecutive k of one r as a
+// 16-byte store (8 rows of 128 bytes per pass).  Requires ld % 4 == 0 and a
+// 16-byte aligned source; R need not be a multiple of 4 (the tail of a
+// row is read element by element).
+__global__ void __launch_bounds__(256)
+k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
+                  __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+  __shared__ float tile[64][65];
+  const int64_t r0 = (int64_t)blockIdx.x * 64, k0 = (int64_t)blockIdx.y * 64;
+  const int t = threadIdx.x;
+  {
+    const int c4 = (t & 15) * 4, kr = t >> 4;  // 16 float4 per 64-wide row, 16 rows per pass
+#pragma unroll
+    for (int j = kr; j < 64; j += 16) {
+      const int64_t k = k0 + j, r = r0 + c4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k < K) {
+        const float* p = src + k * ld + r;
+        if (r + 3 < R) {
+          v = __ldcs(reinterpret_cast<const float4*>(p));
+        } else {
+          if (r < R) v.x = p[0];
+          if (r + 1 < R) v.y = p[1];
+          if (r + 2 < R) v.z = p[2];
+        }
+      }
+      tile[j][c4] = v.x;
+      tile[j][c4 + 1] = v.y;
+      tile[j][c4 + 2] = v.z;
+      tile[j][c4 + 3] = v.w;
+    }
+  }
+  __syncthreads();
+  const int k8 = (t & 7) * 8, rr = t >> 3;  // 8 threads per 64-wide k row, 32 rows per pass
+#pragma unroll
+  for (int j = rr; j < 64; j += 32) {
+    const int64_t r = r0 + j, k = k0 + k8;
+    if (r < R && k < Kp) {  // Kp % 8 == 0, so all 8 are inside the row
+      __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) split_bf16(tile[k8 + q][j], h[q], l[q]);
+      *reinterpret_cast<uint4*>(hi + r * Kp + k) = *reinterpret_cast<const uint4*>(h);
+      if (lo) *reinterpret_cast<uint4*>(lo + r * Kp + k) = *reinterpret_cast<const uint4*>(l);
+    }
+  }
+}
+
+// Fallback for unaligned sources: 32 x 32 tiles, one element per access.
+__global__ void k_split_transpose1(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
+                                   __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
   __shared__ float tile[32][33];
   const int64_t r0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
@@ -404,10 +464,10 @@ __global__ void k_split_transpose(const float* __restrict__ src, int64_t R, int6
   for (int j = ty; j < 32; j += 8) {
     const int64_t r = r0 + j, k = k0 + tx;
     if (r < R && k < Kp) {
-      const float x = tile[tx][j];
-      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      __nv_bfloat16 h, l;
+      split_bf16(tile[tx][j], h, l);
       hi[r * Kp + k] = h;
-      if (lo) lo[r * Kp + k] = __float2bfloat16_rn(x - __bfloat162float(h));
+      if (lo) lo[r * Kp + k] = l;
     }
   }
 }
@@ -417,12 +477,21 @@ __global__ void k_split_transpose(const float* __restrict__ src, int64_t R, int6
 int split_operand(vkc_device_t dev, const float* src, int64_t R, int64_t K, int64_t ld, bool k_contig,
                   __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t Kp) {
   if (k_contig) {
-    unsigned grid = stream_grid(dev, (size_t)(R * Kp), 256);
-    k_split_kmajor<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
+    if (ld % 4 == 0 && ((uintptr_t)src & 15u) == 0) {
+      unsigned grid = wave_grid(dev, k_split_kmajor8, (size_t)(R * (Kp / 8)), 256);
+      k_split_kmajor8<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
+    } else {
+      unsigned grid = stream_grid(dev, (size_t)(R * Kp), 256);
+      k_split_kmajor<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
+    }
+  } else if (ld % 4 == 0 && ((uintptr_t)src & 15u) == 0) {
+    dim3 grid((unsigned)((R + 63) / 64), (unsigned)((Kp + 63) / 64));
+    if (grid.y > 65535) return set_error(VKC_ERR_INVALID, "matmul: K too large for the transpose pre-pass");
+    k_split_transpose<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
   } else {
     dim3 grid((unsigned)((R + 31) / 32), (unsigned)((Kp + 31) / 32));
     if (grid.y > 65535) return set_error(VKC_ERR_INVALID, "matmul: K too large for the transpose pre-pass");
-    k_split_transpose<<<grid, dim3(32, 8), 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
+    k_split_transpose1<<<grid, dim3(32, 8), 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
   }
   return check_launch("split_operand");
 }
@@ -455,23 +524,6 @@ int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t Kp, int bo
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_error(VKC_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return VKC_OK;
-}
-
-template <int BN, bool X3, int STAGES>
-int launch_tc(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
-              const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C, int64_t ldc,
-              const GemmEpilogue& epi) {
-  using Cfg = TcCfg<BN, X3, STAGES>;
-  auto kern = k_gemm_tc<BN, X3, STAGES>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    VKC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
-    attr_set = true;
-  }
-  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + kBM - 1) / kBM));
-  kern<<<grid, kThreadsTC, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
-                                                      epi.bias, epi.act, dev->err_word);
-  return check_launch("gemm_tc");
 }
 
 // ---- split-K tuning table: (precision, log2 buckets of M, N, K) -> splits.
@@ -508,6 +560,59 @@ int choose_splits(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_t
 }
 
 // C = act(alpha * sum_z partial[z] + beta * C + bias), z in order.
+__device__ __forceinline__ float splitk_epilogue(float s, float alpha, float beta, float c, bool has_bias, float bias,
+                                                 int act) {
+  float v = alpha * s;
+  if (beta != 0.f) v += beta * c;
+  if (has_bias) v += bias;
+  if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+  else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+  return v;
+}
+
+__device__ __forceinline__ void add4(float4& s, const float4& a) {
+  s.x += a.x;
+  s.y += a.y;
+  s.z += a.z;
+  s.w += a.w;
+}
+
+// Four columns per thread (N % 4 == 0, ldc % 4 == 0, 16-byte aligned C);
+// the split loads are issued four at a time ahead of their (ordered) adds.
+__global__ void __launch_bounds__(256)
+k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
+                 float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
+  const int64_t total = M * N, quads = total / 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += stride) {
+    const int64_t i = q * 4;
+    const float4* p = reinterpret_cast<const float4*>(partial + i);
+    float4 s = __ldcs(p);
+    int z = 1;
+    for (; z + 3 < splits; z += 4) {
+      const float4 a = __ldcs(p + (int64_t)z * quads), b = __ldcs(p + (int64_t)(z + 1) * quads);
+      const float4 c = __ldcs(p + (int64_t)(z + 2) * quads), d = __ldcs(p + (int64_t)(z + 3) * quads);
+      add4(s, a);
+      add4(s, b);
+      add4(s, c);
+      add4(s, d);
+    }
+    for (; z < splits; ++z) add4(s, __ldcs(p + (int64_t)z * quads));
+    const int64_t r = i / N, col = i - r * N;
+    float4* cp = reinterpret_cast<float4*>(C + r * ldc + col);
+    const float4 c0 = beta != 0.f ? *cp : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 b4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (bias) b4 = make_float4(bias[col], bias[col + 1], bias[col + 2], bias[col + 3]);
+    float4 v;
+    const bool hb = bias != nullptr;
+    v.x = splitk_epilogue(s.x, alpha, beta, c0.x, hb, b4.x, act);
+    v.y = splitk_epilogue(s.y, alpha, beta, c0.y, hb, b4.y, act);
+    v.z = splitk_epilogue(s.z, alpha, beta, c0.z, hb, b4.z, act);
+    v.w = splitk_epilogue(s.w, alpha, beta, c0.w, hb, b4.w, act);
+    *cp = v;
+  }
+}
+
 __global__ void __launch_bounds__(256)
 k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
                 float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
@@ -518,31 +623,66 @@ k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_
     for (int z = 1; z < splits; ++z) s += partial[(int64_t)z * total + i];
     const int64_t r = i / N, col = i - r * N;
     float* c = C + r * ldc + col;
-    float v = alpha * s;
-    if (beta != 0.f) v += beta * *c;
-    if (bias) v += bias[col];
-    if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
-    else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-    *c = v;
+    *c = splitk_epilogue(s, alpha, beta, beta != 0.f ? *c : 0.f, bias != nullptr, bias ? bias[col] : 0.f, act);
   }
 }
 
-template <int STAGES>
-int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
-                 const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C,
-                 int64_t ldc, const GemmEpilogue& epi) {
-  using Cfg = TcCfg<128, true, STAGES>;
-  auto kern = k_gemm_tc_x3<STAGES>;
+int splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M, int64_t N, float alpha, float beta,
+                  float* C, int64_t ldc, const GemmEpilogue& epi) {
+  if (N % 4 == 0 && ldc % 4 == 0 && ((uintptr_t)C & 15u) == 0) {
+    unsigned g = wave_grid(dev, k_splitk_reduce4, (size_t)(M * N / 4), 256);
+    k_splitk_reduce4<<<g, 256, 0, dev->stream>>>(partial, splits, M, N, alpha, beta, C, ldc, epi.bias, epi.act);
+  } else {
+    unsigned g = stream_grid(dev, (size_t)(M * N), 256);
+    k_splitk_reduce<<<g, 256, 0, dev->stream>>>(partial, splits, M, N, alpha, beta, C, ldc, epi.bias, epi.act);
+  }
+  return check_launch("splitk_reduce");
+}
+
+// Clusters of this kernel that fit on the device at once (cached).
+template <class Kern>
+int max_clusters(vkc_device_t dev, Kern kern, uint32_t smem) {
+  static int cached = 0;
+  if (cached > 0) return cached;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * (unsigned)dev->sm_count, 1, 1);
+  cfg.blockDim = dim3(kThreadsP, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    n = dev->sm_count / 2;
+  }
+  cached = n;
+  return n;
+}
+
+template <bool X3, int STAGES, int DRAIN>
+int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
+               const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C,
+               int64_t ldc, const GemmEpilogue& epi) {
+  using Cfg = PCfg<X3, STAGES>;
+  auto kern = k_gemm_tcp<X3, STAGES, DRAIN>;
   static bool attr_set = false;
   if (!attr_set) {
     VKC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
     attr_set = true;
   }
-  const int64_t tiles = ((N + 127) / 128) * ((M + kBM - 1) / kBM);
+  const int64_t m_blocks = (M + kBM - 1) / kBM;
+  const int m_pairs = (int)((m_blocks + 1) / 2);
+  const int n_blocks = (int)((N + kBN2 - 1) / kBN2);
+  const int64_t tiles = (int64_t)m_pairs * n_blocks;
   const int nk = (int)((K + kBK - 1) / kBK);
-  // Split K when the tiles alone would leave most SMs idle (tuning table
-  // first, then the occupancy heuristic); no empty split.
-  int splits = choose_splits(dev, VKC_MM_BF16X3, M, N, K, tiles, nk);
+  // Split K when the 256 x 256 units alone would leave most SMs idle (tuning
+  // table first, then the occupancy heuristic); no empty split.
+  int splits = choose_splits(dev, X3 ? VKC_MM_BF16X3 : VKC_MM_BF16, M, N, K, 2 * tiles, nk);
   const int kps = (nk + splits - 1) / splits;
   splits = (nk + kps - 1) / kps;
   float* partial = nullptr;
@@ -550,15 +690,25 @@ int launch_tc_x3(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb,
     int r = scratch_alloc(dev, sizeof(float) * (size_t)splits * M * N, (void**)&partial);
     if (r != VKC_OK) return r;
   }
-  dim3 grid((unsigned)((N + 127) / 128), (unsigned)((M + kBM - 1) / kBM), (unsigned)splits);
-  kern<<<grid, kThreadsTC, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
-                                                      epi.bias, epi.act, dev->err_word, partial, kps);
-  int r = check_launch("gemm_tc_x3");
-  if (r == VKC_OK && splits > 1) {
-    unsigned g = stream_grid(dev, (size_t)(M * N), 256);
-    k_splitk_reduce<<<g, 256, 0, dev->stream>>>(partial, splits, M, N, alpha, beta, C, ldc, epi.bias, epi.act);
-    r = check_launch("splitk_reduce");
-  }
+  const int64_t units = tiles * splits;
+  const int clusters = (int)std::min<int64_t>(units, max_clusters(dev, kern, Cfg::kSmem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * (unsigned)clusters, 1, 1);
+  cfg.blockDim = dim3(kThreadsP, 1, 1);
+  cfg.dynamicSmemBytes = Cfg::kSmem;
+  cfg.stream = dev->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
+                                     epi.bias, epi.act, dev->err_word, partial, splits, kps, m_pairs, n_blocks);
+  int r = e == cudaSuccess ? check_launch("gemm_tc") : set_error(VKC_ERR_CUDA, "gemm_tc launch: %s",
+                                                                  cudaGetErrorString(e));
+  if (r == VKC_OK && splits > 1) r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
   scratch_free(dev, partial);
   return r;
 }
@@ -578,7 +728,7 @@ VKC_EXPORT int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k,
 
 VKC_EXPORT int vkc_gemm_tune_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits) {
   VKC_REQUIRE(dev && splits, "NULL argument");
-  const int64_t tiles = ((n + 127) / 128) * ((m + 127) / 128);
+  const int64_t tiles = 2 * (((m + 127) / 128 + 1) / 2) * ((n + 255) / 256);  // CTA tiles, 128 x 256
   const int nk = (int)((k + 63) / 64);
   *splits = vkc::choose_splits(dev, precision, m, n, k, tiles, nk);
   return VKC_OK;
@@ -600,7 +750,10 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   VKC_REQUIRE(M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), "matmul dimension too large");
   VKC_REQUIRE((M + kBM - 1) / kBM <= 65535, "matmul: M too large for the tensor-core grid");
   const bool x3 = precision == VKC_MM_BF16X3;
-  const int64_t Kp = (K + 7) / 8 * 8;  // 16-byte aligned rows for TMA
+  // Rows padded with zeros to whole 64-wide K blocks: every TMA box is then
+  // inside the operand along K (a box reaching past a short row, e.g. K = 10,
+  // made the whole GEMM several times slower).
+  const int64_t Kp = (K + kBK - 1) / kBK * kBK;
   const size_t a_elems = (size_t)M * Kp, b_elems = (size_t)N * Kp;
   const size_t bytes = (a_elems + b_elems) * sizeof(__nv_bfloat16) * (x3 ? 2 : 1);
   void* scratch = nullptr;
@@ -614,15 +767,16 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   // op(B)(k,n): tb ? B[n*ldb + k] : B[k*ldb + n]  -> (n,k) K contiguous iff tb
   r = split_operand(dev, A, M, K, lda, !ta, a_hi, a_lo, Kp);
   if (r == VKC_OK) r = split_operand(dev, B, N, K, ldb, tb, b_hi, b_lo, Kp);
+  // every box is 128 rows x 64 K: a CTA's op(A) tile or one half of the
+  // 256-row op(B) tile
   CUtensorMap ma, mb, malo, mblo;
-  const int bn = x3 ? 128 : 256;
   if (r == VKC_OK) r = make_map(&ma, a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, bn);
+  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, 128);
   if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, bn);
+  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, 128);
   if (r == VKC_OK) {
-    if (x3) r = launch_tc_x3<3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
-    else r = launch_tc<256, false, 4>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
+    if (x3) r = launch_tcp<true, 2, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
+    else r = launch_tcp<false, 4, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
   }
   scratch_free(dev, scratch);
   return r;

@@ -15,9 +15,11 @@
 // MMA descriptors expect (tile (r, k): row r's 16-byte chunk c at byte
 // r*128 + ((c ^ (r & 7)) << 4)), so one untiled bulk copy per operand tile
 // fills a pipeline stage -- no tensor maps, whose per-problem encoding would
-// not fit a launch.  The MMA and epilogue follow k_gemm_tc_x3 (one TMEM
-// buffer per 64-wide K block, drained into fp32 registers), so split-bf16x3
-// results are bit-identical to vkc_gemm when that call does not split K.
+// not fit a launch.  The MMA and epilogue follow k_gemm_tcp (split mode: one
+// TMEM accumulation per kDrainX3 K blocks, drained into fp32 registers in
+// order), so split-bf16x3 results are bit-identical to vkc_gemm when that call
+// does not split K.
+#include "colsum.cuh"
 #include "gemm_simt.cuh"
 #include "tc_ptx.cuh"
 
@@ -282,33 +284,38 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
     // ---------------- MMA issuer
     constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                ((uint32_t)(kTileRows >> 4) << 24);
-    uint32_t g = 0;
+    uint32_t g = 0, acc = 0;  // g: K blocks (stage ring), acc: accumulations (TMEM ring)
     bool ok = true;
     for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
       const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
-      for (int kb = 0; kb < P.kt; ++kb, ++g) {
-        const int s = g % S, b = g % kAccBufs;
-        if (*abort_flag || !mbar_wait(full_bar(s), (g / S) & 1) ||
-            !mbar_wait(acce_bar(b), ((g / kAccBufs) & 1) ^ 1)) {
-          ok = false;
-          break;
-        }
+      const int span = X3 ? kDrainX3 : P.kt;  // K blocks per TMEM accumulation
+      for (int g0 = 0; g0 < P.kt && ok; g0 += span, ++acc) {
+        const int b = acc % kAccBufs;
+        if (*abort_flag || !mbar_wait(acce_bar(b), ((acc / kAccBufs) & 1) ^ 1)) { ok = false; break; }
         tc_fence_after();
         const uint32_t d = tmem + (uint32_t)(b * BN);
+        const int g1 = min(P.kt, g0 + span);
+        for (int kb = g0; kb < g1; ++kb, ++g) {
+          const int s = g % S;
+          if (*abort_flag || !mbar_wait(full_bar(s), (g / S) & 1)) { ok = false; break; }
+          tc_fence_after();
 #pragma unroll
-        for (int k = 0; k < kTileK / 16; ++k) {
-          const uint64_t a = sw128_desc(stage(s, 0) + 32u * k);
-          const uint64_t bb = sw128_desc(stage(s, 1) + 32u * k);
-          if (X3) {
-            // the same order as k_gemm_tc_x3: cross terms, then hi*hi
-            mma_bf16(d, a, sw128_desc(stage(s, 3) + 32u * k), idesc, k != 0);
-            mma_bf16(d, sw128_desc(stage(s, 2) + 32u * k), bb, idesc, 1);
-            mma_bf16(d, a, bb, idesc, 1);
-          } else {
-            mma_bf16(d, a, bb, idesc, k != 0);
+          for (int k = 0; k < kTileK / 16; ++k) {
+            const uint64_t a = sw128_desc(stage(s, 0) + 32u * k);
+            const uint64_t bb = sw128_desc(stage(s, 1) + 32u * k);
+            const uint32_t first = (kb == g0 && k == 0) ? 0u : 1u;
+            if (X3) {
+              // the same order as k_gemm_tcp: cross terms, then hi*hi
+              mma_bf16(d, a, sw128_desc(stage(s, 3) + 32u * k), idesc, first);
+              mma_bf16(d, sw128_desc(stage(s, 2) + 32u * k), bb, idesc, 1);
+              mma_bf16(d, a, bb, idesc, 1);
+            } else {
+              mma_bf16(d, a, bb, idesc, first);
+            }
           }
+          mma_commit(empty_bar(s));
         }
-        mma_commit(empty_bar(s));
+        if (!ok) break;
         mma_commit(accf_bar(b));
       }
     }
@@ -317,51 +324,79 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
       *abort_flag = 1;
     }
   } else if (warp >= 2) {
-    // ---------------- epilogue: drain every K block into fp32 registers
+    // ---------------- epilogue: accumulations -> fp32 registers -> global
+    // The sums go back into the last accumulation's TMEM buffer and the store
+    // loop reads them 32 columns at a time (not unrolled), so the epilogue
+    // code exists once instead of 128 times (instruction fetch dominated
+    // small launches with the unrolled form).
     const int q = warp & 3;
+    const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
     uint32_t g = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
       const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
       const int local = t - P.tile0;
       const int m0 = (local / P.tiles_n) * kTileRows, n0 = (local % P.tiles_n) * BN;
-      float sum[BN];
+      const int span = X3 ? kDrainX3 : P.kt;
+      const int ngroups = (P.kt + span - 1) / span;
+      float sum[X3 ? BN : 1];
+      if (X3) {
 #pragma unroll
-      for (int j = 0; j < BN; ++j) sum[j] = 0.f;
-      for (int kb = 0; kb < P.kt; ++kb, ++g) {
-        const int b = g % kAccBufs;
+        for (int j = 0; j < (X3 ? BN : 1); ++j) sum[j] = 0.f;
+      }
+      int b = 0;
+      for (int gi = 0; gi < ngroups; ++gi, ++g) {
+        b = g % kAccBufs;
         if (*abort_flag || !mbar_wait(accf_bar(b), (g / kAccBufs) & 1)) { ok = false; break; }
         tc_fence_after();
+        if (X3) {
+          const bool last = gi == ngroups - 1;
 #pragma unroll
-        for (int c = 0; c < BN / 32; ++c) {
-          uint32_t r[32];
-          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + c * 32), r);
+          for (int c = 0; c < BN / 32; ++c) {
+            const uint32_t ta = tmem + lane_addr + (uint32_t)(b * BN + c * 32);
+            uint32_t r[32];
+            tmem_ld32(ta, r);
 #pragma unroll
-          for (int j = 0; j < 32; ++j) sum[c * 32 + j] += __uint_as_float(r[j]);
+            for (int j = 0; j < 32; ++j) {
+              sum[(X3 ? c * 32 + j : 0)] += __uint_as_float(r[j]);
+              r[j] = __float_as_uint(sum[(X3 ? c * 32 + j : 0)]);
+            }
+            if (last) tmem_st32(ta, r);
+          }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(acce_bar(b));
+        if (gi + 1 < ngroups) {
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(acce_bar(b));
+        }
       }
       if (!ok) break;
       const int row = m0 + q * 32 + lane;
-      if (row < P.m) {
-        float* crow = P.c + (int64_t)row * P.ldc;
-        const float* mrow = P.mask ? P.mask + (int64_t)row * P.ldc : nullptr;
+      float* crow = P.c + (int64_t)row * P.ldc;
+      const float* mrow = P.mask ? P.mask + (int64_t)row * P.ldc : nullptr;
+#pragma unroll 1
+      for (int c = 0; c < BN / 32; ++c) {
+        uint32_t r[32];
+        tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r);
+        if (row < P.m) {
 #pragma unroll
-        for (int j = 0; j < BN; ++j) {  // fully unrolled: sum[] stays in registers
-          const int col = n0 + j;
-          if (col < P.n) {
-            float v = P.alpha * sum[j];
-            if (P.beta != 0.f) v += P.beta * crow[col];
-            if (P.bias) v += P.bias[col];
-            if (P.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
-            else if (P.act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-            if (mrow) v = relu_mask(v, mrow[col]);
-            crow[col] = v;
+          for (int j = 0; j < 32; ++j) {
+            const int col = n0 + c * 32 + j;
+            if (col < P.n) {
+              float v = P.alpha * __uint_as_float(r[j]);
+              if (P.beta != 0.f) v += P.beta * crow[col];
+              if (P.bias) v += P.bias[col];
+              if (P.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+              else if (P.act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+              if (mrow) v = relu_mask(v, mrow[col]);
+              crow[col] = v;
+            }
           }
         }
       }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce_bar(b));
     }
     if (!ok) {
       if (lane == 0) atomicOr(err, 2u);
@@ -389,7 +424,7 @@ struct ColsumItem {
   const float* dy;
   float* db;
   int64_t batch, cols;
-  int block0;  // first block of this item (blocks of 256 columns)
+  int block0;  // first block of this item (blocks of 32 columns)
 };
 struct ColsumTable {
   int count, total, overwrite;
@@ -400,6 +435,7 @@ struct ColsumTable {
 // bias-gradient kernel.  `overwrite`: db[o] = the sum, which equals adding it
 // to a zeroed gradient (the sum starts at +0, so it is never -0).
 __global__ void __launch_bounds__(256) k_colsum_grouped(const __grid_constant__ ColsumTable tab) {
+  __shared__ float tile[kColsumRows][kColsumCols + 1];
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
     int lo = 0, hi = tab.count - 1;
     while (lo < hi) {
@@ -408,13 +444,10 @@ __global__ void __launch_bounds__(256) k_colsum_grouped(const __grid_constant__ 
       else hi = mid - 1;
     }
     const ColsumItem& I = tab.it[lo];
-    const int64_t o = (int64_t)(t - I.block0) * 256 + threadIdx.x;
-    if (o < I.cols) {
-      float s = 0.f;
-#pragma unroll 8
-      for (int64_t b = 0; b < I.batch; ++b) s += I.dy[b * I.cols + o];  // loads run ahead, adds in order
-      I.db[o] = tab.overwrite ? s : I.db[o] + s;
-    }
+    const int64_t c0 = (int64_t)(t - I.block0) * kColsumCols;
+    const float s = colsum32(I.dy, I.batch, I.cols, I.cols, c0, tile);
+    const int64_t o = c0 + threadIdx.x;
+    if (threadIdx.x < 32 && o < I.cols) I.db[o] = tab.overwrite ? s : I.db[o] + s;
   }
 }
 
@@ -712,7 +745,7 @@ VKC_EXPORT int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, floa
       I.batch = batch[i];
       I.cols = cols[i];
       I.block0 = total;
-      total += (int)((cols[i] + 255) / 256);
+      total += (int)((cols[i] + kColsumCols - 1) / kColsumCols);
     }
     tab.total = total;
     if (total == 0) continue;

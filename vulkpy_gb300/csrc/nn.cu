@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "gemm_simt.cuh"
 #include "gemm_tc.cuh"
+#include "colsum.cuh"
 
 namespace {
 
@@ -29,14 +30,13 @@ int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64
   return vkc::set_error(VKC_ERR_INVALID, "unknown matmul precision %d", precision);
 }
 
-// db[o] += sum_b dy[b, o]
-__global__ void k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
-  int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= out_dim) return;
-  float s = 0.f;
-#pragma unroll 8
-  for (int64_t b = 0; b < batch; ++b) s += dy[b * out_dim + o];  // loads run ahead, adds in order
-  db[o] += s;
+// db[o] += sum_b dy[b, o], b in order (one block per 32 columns).
+__global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
+  __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
+  const int64_t c0 = (int64_t)blockIdx.x * vkc::kColsumCols;
+  const float s = vkc::colsum32(dy, batch, out_dim, out_dim, c0, tile);
+  const int64_t o = c0 + threadIdx.x;
+  if (threadIdx.x < 32 && o < out_dim) db[o] += s;
 }
 
 __device__ __forceinline__ float warp_max(float v) {
@@ -248,8 +248,8 @@ VKC_EXPORT int vkc_dense_backward(vkc_device_t dev, int precision, const float* 
   VKC_REQUIRE(x && w && dy, "NULL buffer");
   int r = VKC_OK;
   if (db) {
-    unsigned grid = (unsigned)((out_dim + kThreads - 1) / kThreads);
-    k_colsum_acc<<<grid, kThreads, 0, dev->stream>>>(dy, batch, out_dim, db);
+    unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
+    k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db);
     r = vkc::check_launch("dense_backward db");
     if (r != VKC_OK) return r;
   }

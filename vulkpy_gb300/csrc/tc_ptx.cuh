@@ -116,8 +116,79 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
 
 constexpr int kAccBufs = 4;
 
+// Split-bf16x3: K blocks (64 wide) per TMEM accumulation.  The tensor pipe
+// adds into its fp32 accumulator with truncation, so one accumulation over
+// all of K loses accuracy as K grows (2.9e-5 relative at K = 8192 on N(0,1)
+// data); restarting it every kDrainX3 blocks and adding the partials in fp32
+// registers bounds that loss.  Measured at K = 8192 (relative Frobenius error
+// vs float64; 1 / 2 / 4 / 8 / 16 blocks): N(0,1) data 4.46 / 4.47 / 4.53 /
+// 4.76 / 5.59 e-6, U[0,1) data 0.24 / 0.38 / 0.78 / 1.66 / 3.62 e-6.  Each
+// drain reads the whole accumulator out of TMEM, which slows the tensor pipe,
+// so fewer drains are faster (8192^3: 398 / 432 / 439 / 457 / 499 TFLOP/s).
+constexpr int kDrainX3 = 8;
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+}  // namespace
+}  // namespace vkc
+
+// ------------------------------------------------------------ cluster helpers
+namespace vkc {
+namespace {
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// All threads of every CTA in the cluster: release this CTA's prior shared
+// memory writes (barrier inits) to the cluster and wait for the others.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// 2-D TMA load delivered to the same shared-memory offset (and completing on
+// the mbarrier at the same offset) in every CTA of `mask`.
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask)
+      : "memory");
+}
+
+// Arrive (once) on the mbarrier at offset `bar` of every CTA in `mask` when
+// all tcgen05 operations issued so far by this thread have completed.
+__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+      "h"(mask)
+      : "memory");
+}
+
+}  // namespace
+}  // namespace vkc
+
+namespace vkc {
+namespace {
+
+// 32 lanes x 32 consecutive 32-bit columns from registers into TMEM (the
+// inverse of tmem_ld32), completed before returning.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+      "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+      "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+      "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 }  // namespace
