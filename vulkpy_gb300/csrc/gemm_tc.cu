@@ -189,6 +189,12 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
+    if (X3) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_alo)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_blo)) : "memory");
+    }
     int it = 0;
     bool ok = true;
     for (int u = cluster; u < units && ok; u += nclusters) {
@@ -295,17 +301,25 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
           // the sums back into the buffer for the store loop below
           const bool last = gi == ngroups - 1;
 #pragma unroll
-          for (int c = 0; c < 4; ++c) {
+          for (int c = 0; c < 4; c += 2) {
             const uint32_t ta = tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32);
-            uint32_t r[32];
-            tmem_ld32(ta, r);
+            uint32_t r0[32], r1[32];
+            tmem_ld32_nw(ta, r0);
+            tmem_ld32_nw(ta + 32, r1);
+            tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-              acc[(X3 ? c * 32 + j : 0)] += __uint_as_float(r[j]);
-              r[j] = __float_as_uint(acc[(X3 ? c * 32 + j : 0)]);
+              acc[(X3 ? c * 32 + j : 0)] += __uint_as_float(r0[j]);
+              r0[j] = __float_as_uint(acc[(X3 ? c * 32 + j : 0)]);
+              acc[(X3 ? c * 32 + 32 + j : 0)] += __uint_as_float(r1[j]);
+              r1[j] = __float_as_uint(acc[(X3 ? c * 32 + 32 + j : 0)]);
             }
-            if (last) tmem_st32(ta, r);
+            if (last) {
+              tmem_st32_nw(ta, r0);
+              tmem_st32_nw(ta + 32, r1);
+            }
           }
+          if (last) tmem_wait_st();
         }
         if (gi + 1 < ngroups) {
           tc_fence_before();
@@ -319,12 +333,17 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
       const bool raw_out = partial != nullptr;
       float* crow = raw_out ? partial + ((int64_t)p.z * M + row) * N : C + (int64_t)row * ldc;
 #pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        uint32_t r[32];
-        tmem_ld32(tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32), r);
+      for (int c = 0; c < 4; c += 2) {
+        const uint32_t ta = tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32);
+        uint32_t r0[32], r1[32];
+        tmem_ld32_nw(ta, r0);
+        tmem_ld32_nw(ta + 32, r1);
+        tmem_wait_ld();
         const int col0 = p.n0 + h * 128 + c * 32;
         if (row < M && col0 < N)
-          store_row32(reinterpret_cast<const float*>(r), crow, bias, col0, N, alpha, beta, act, raw_out);
+          store_row32(reinterpret_cast<const float*>(r0), crow, bias, col0, N, alpha, beta, act, raw_out);
+        if (row < M && col0 + 32 < N)
+          store_row32(reinterpret_cast<const float*>(r1), crow, bias, col0 + 32, N, alpha, beta, act, raw_out);
       }
       tc_fence_before();
       __syncwarp();

@@ -352,17 +352,25 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
         if (X3) {
           const bool last = gi == ngroups - 1;
 #pragma unroll
-          for (int c = 0; c < BN / 32; ++c) {
+          for (int c = 0; c < BN / 32; c += 2) {
             const uint32_t ta = tmem + lane_addr + (uint32_t)(b * BN + c * 32);
-            uint32_t r[32];
-            tmem_ld32(ta, r);
+            uint32_t r0[32], r1[32];
+            tmem_ld32_nw(ta, r0);
+            tmem_ld32_nw(ta + 32, r1);
+            tmem_wait_ld();
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
-              sum[(X3 ? c * 32 + j : 0)] += __uint_as_float(r[j]);
-              r[j] = __float_as_uint(sum[(X3 ? c * 32 + j : 0)]);
+              sum[(X3 ? c * 32 + j : 0)] += __uint_as_float(r0[j]);
+              r0[j] = __float_as_uint(sum[(X3 ? c * 32 + j : 0)]);
+              sum[(X3 ? c * 32 + 32 + j : 0)] += __uint_as_float(r1[j]);
+              r1[j] = __float_as_uint(sum[(X3 ? c * 32 + 32 + j : 0)]);
             }
-            if (last) tmem_st32(ta, r);
+            if (last) {
+              tmem_st32_nw(ta, r0);
+              tmem_st32_nw(ta + 32, r1);
+            }
           }
+          if (last) tmem_wait_st();
         }
         if (gi + 1 < ngroups) {
           tc_fence_before();
@@ -375,15 +383,17 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
       float* crow = P.c + (int64_t)row * P.ldc;
       const float* mrow = P.mask ? P.mask + (int64_t)row * P.ldc : nullptr;
 #pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {
-        uint32_t r[32];
-        tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r);
+      for (int c = 0; c < BN / 32; c += 2) {
+        uint32_t r[2][32];
+        tmem_ld32_nw(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r[0]);
+        tmem_ld32_nw(tmem + lane_addr + (uint32_t)(b * BN + c * 32 + 32), r[1]);
+        tmem_wait_ld();
         if (row < P.m) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
+          for (int j = 0; j < 64; ++j) {
             const int col = n0 + c * 32 + j;
             if (col < P.n) {
-              float v = P.alpha * __uint_as_float(r[j]);
+              float v = P.alpha * __uint_as_float(r[j >> 5][j & 31]);
               if (P.beta != 0.f) v += P.beta * crow[col];
               if (P.bias) v += P.bias[col];
               if (P.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
