@@ -247,11 +247,17 @@ int vkc_gemm(vkc_device_t dev, int precision, int trans_a, int trans_b,
              const float* a, int64_t lda, const float* b, int64_t ldb,
              float beta, float* c, int64_t ldc);
 
-/* Split-K tuning table of the tensor-core GEMM, keyed by precision and the
- * log2 size buckets of (m, n, k); splits = 0 removes an entry.  The table
- * written by vulkpy_gb300/autotune.py is loaded at import; shapes without an
- * entry use an occupancy heuristic.  get: the split count a shape will use.
- * No reference counterpart (matmul.comp has no tiling). */
+/* Tuning table of the tensor-core GEMM, keyed by precision and the log2 size
+ * buckets of (m, n, k): the CTA tile width (tile_n = 128 or 256 columns of C
+ * per 128-row tile) and the split-K count; splits = 0 removes an entry.  The
+ * table written by vulkpy_gb300/autotune.py is loaded at import; shapes
+ * without an entry use 256-wide tiles and an occupancy heuristic for splits.
+ * get: the plan a shape will use.  tune_set/tune_get are the same with
+ * tile_n = 256 / without it.  No reference counterpart (matmul.comp has no
+ * tiling). */
+int vkc_gemm_plan_set(int precision, int64_t m, int64_t n, int64_t k, int splits, int tile_n);
+int vkc_gemm_plan_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits,
+                      int* tile_n);
 int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k, int splits);
 int vkc_gemm_tune_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits);
 int vkc_gemm_tune_clear(void);

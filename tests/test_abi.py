@@ -55,9 +55,12 @@ def test_gemm_tuning_table_host_side(tmp_path):
     assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 256, 1024, 784, 65) == _lib.ERR_INVALID
     assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 256, 1024, 784, 4) == _lib.OK
     assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, 256, 1024, 784, 0) == _lib.OK   # erase
+    assert _lib.lib.vkc_gemm_plan_set(_lib.MM_BF16, 256, 1024, 784, 4, 96) == _lib.ERR_INVALID
+    assert _lib.lib.vkc_gemm_plan_set(_lib.MM_BF16, 256, 1024, 784, 4, 128) == _lib.OK
+    assert _lib.lib.vkc_gemm_plan_set(_lib.MM_BF16, 256, 1024, 784, 0, 128) == _lib.OK   # erase
     p = tmp_path / "t.json"
-    p.write_text(json.dumps({"bf16x3": [[8, 10, 10, 2], [7, 12, 14, 8]]}))
-    assert autotune.load_table(str(p)) == 2
+    p.write_text(json.dumps({"bf16x3": [[8, 10, 10, 2], [7, 12, 14, 8, 128]], "bf16": [[8, 10, 10, 3, 256]]}))
+    assert autotune.load_table(str(p)) == 3
     assert _lib.lib.vkc_gemm_tune_clear() == _lib.OK
     autotune.load_table()   # restore the shipped table
     assert autotune.bucket(1) == 0 and autotune.bucket(784) == 10 and autotune.bucket(1024) == 10

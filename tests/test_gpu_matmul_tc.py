@@ -80,35 +80,45 @@ def test_dense_layer_on_tensor_cores(gpu, vk):
     assert gpu.check_errors() == 0
 
 
-@pytest.mark.parametrize("m,n,k", [(256, 1024, 784), (64, 300, 2000), (1, 37, 4096)])
-def test_split_k_counts_agree(gpu, vk, m, n, k):
-    """Every split count the tuner may choose gives the bf16x3 accuracy, the
-    table's choice is the one used, and a fixed choice is bit-reproducible."""
+@pytest.mark.parametrize("m,n,k", [(256, 1024, 784), (64, 300, 2000), (1, 37, 4096), (385, 200, 130)])
+@pytest.mark.parametrize("prec,bound", [("bf16x3", 1e-5), ("bf16", 8e-3)])
+def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
+    """Every plan the tuner may choose (tile width 256 or 128 x split count)
+    gives the precision's accuracy, the table's choice is the one used, and a
+    fixed choice is bit-reproducible.  In split mode all plans give the same
+    bits when K is not split (the per-element accumulation does not depend on
+    the tile width)."""
     import ctypes as C
     from vulkpy_gb300 import _lib
+    P = {"bf16x3": _lib.MM_BF16X3, "bf16": _lib.MM_BF16}[prec]
     rng = np.random.default_rng(m + n + k)
     A = rng.standard_normal((m, k)).astype(np.float32)
     B = rng.standard_normal((n, k)).astype(np.float32)
     a, b = vk.Array(gpu, data=A), vk.Array(gpu, data=B)
     exp = A.astype(np.float64) @ B.T.astype(np.float64)
+    unsplit = []
     try:
-        for s in (1, 2, 3, 8, 16):
-            assert _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, s) == 0
-            got = C.c_int()
-            assert _lib.lib.vkc_gemm_tune_get(gpu.handle, _lib.MM_BF16X3, m, n, k, C.byref(got)) == 0
-            assert got.value == min(s, (k + 63) // 64)
-            outs = []
-            for _ in range(2):
-                c = vk.Array(gpu, shape=(m, n))
-                st = _lib.lib.vkc_gemm(gpu.handle, _lib.MM_BF16X3, 0, 1, m, n, k, C.c_float(1.0), a._dptr(), k,
-                                       b._dptr(), k, C.c_float(0.0), c._dptr(), n)
-                assert st == 0, _lib.last_error()
-                c._written()
-                outs.append(np.asarray(c).copy())
-            assert np.array_equal(outs[0], outs[1]), s
-            assert rel_fro(outs[0], exp) < 1e-5, s
+        for tile in (256, 128):
+            for s in (1, 2, 3, 8, 16):
+                assert _lib.lib.vkc_gemm_plan_set(P, m, n, k, s, tile) == 0
+                got, got_tile = C.c_int(), C.c_int()
+                assert _lib.lib.vkc_gemm_plan_get(gpu.handle, P, m, n, k, C.byref(got), C.byref(got_tile)) == 0
+                assert got.value == min(s, (k + 63) // 64) and got_tile.value == tile
+                outs = []
+                for _ in range(2):
+                    c = vk.Array(gpu, shape=(m, n))
+                    st = _lib.lib.vkc_gemm(gpu.handle, P, 0, 1, m, n, k, C.c_float(1.0), a._dptr(), k,
+                                           b._dptr(), k, C.c_float(0.0), c._dptr(), n)
+                    assert st == 0, _lib.last_error()
+                    c._written()
+                    outs.append(np.asarray(c).copy())
+                assert np.array_equal(outs[0], outs[1]), (tile, s)
+                assert rel_fro(outs[0], exp) < bound, (tile, s)
+                if s == 1:
+                    unsplit.append(outs[0])
+        np.testing.assert_array_equal(unsplit[0], unsplit[1])
     finally:
-        _lib.lib.vkc_gemm_tune_set(_lib.MM_BF16X3, m, n, k, 0)
+        _lib.lib.vkc_gemm_tune_set(P, m, n, k, 0)
         from vulkpy_gb300 import autotune
         autotune.load_table()
     assert gpu.check_errors() == 0

@@ -93,6 +93,8 @@ _SIGS = {
     "vkc_reduce_all_noalloc": ([vp, i32, i32, vp, sz, vp, f32], i32),
     "vkc_matmul": ([vp, i32, vp, vp, vp, i64, i64, i64], i32),
     "vkc_gemm": ([vp, i32, i32, i32, i64, i64, i64, f32, vp, i64, vp, i64, f32, vp, i64], i32),
+    "vkc_gemm_plan_set": ([i32, i64, i64, i64, i32, i32], i32),
+    "vkc_gemm_plan_get": ([vp, i32, i64, i64, i64, C.POINTER(C.c_int), C.POINTER(C.c_int)], i32),
     "vkc_gemm_tune_set": ([i32, i64, i64, i64, i32], i32),
     "vkc_gemm_tune_get": ([vp, i32, i64, i64, i64, C.POINTER(C.c_int)], i32),
     "vkc_gemm_tune_clear": ([], i32),

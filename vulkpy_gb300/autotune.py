@@ -1,9 +1,10 @@
 """
-Split-K autotuner for the tensor-core GEMM (bf16 and split-bf16x3).
+Autotuner for the tensor-core GEMM (bf16 and split-bf16x3): CTA tile width
+and split-K count.
 
 For each size bucket (ceil(log2) of M, N and K) the tuner times every
-candidate split count on a representative problem of that bucket and keeps
-the fastest.  The result is written to ``tuning.json`` next to this file and
+candidate (tile width 256 or 128, split count) on a representative problem of
+that bucket and keeps the fastest.  The result is written to ``tuning.json`` next to this file and
 loaded into the library at import (vkc_gemm_tune_set), so the choice at run
 time is a table lookup: deterministic, the same in eager runs and graph
 captures.  Buckets without an entry fall back to an occupancy heuristic.
@@ -26,7 +27,8 @@ from . import _lib
 from ._lib import lib, check
 
 TABLE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
-CANDIDATES = (1, 2, 3, 4, 6, 8, 12, 16)
+CANDIDATES = (1, 2, 3, 4, 6, 8, 12, 16)   # split-K counts
+TILES = (256, 128)                         # CTA tile widths (columns of C)
 
 
 def bucket(x: int) -> int:
@@ -44,9 +46,11 @@ def load_table(path: str = TABLE_PATH) -> int:
         data = json.load(f)
     n = 0
     for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16)):
-        for m, nn, k, splits in data.get(name, []):
+        for entry in data.get(name, []):
+            m, nn, k, splits = entry[:4]
+            tile = int(entry[4]) if len(entry) > 4 else 256
             # representative sizes: the top of each bucket
-            check(lib.vkc_gemm_tune_set(prec, 1 << m, 1 << nn, 1 << k, int(splits)))
+            check(lib.vkc_gemm_plan_set(prec, 1 << m, 1 << nn, 1 << k, int(splits), tile))
             n += 1
     return n
 
@@ -130,24 +134,26 @@ def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) ->
             B = vk.Array(gpu, data=rng.standard_normal((n, k)).astype(np.float32))
             Cm = vk.Array(gpu, shape=(m, n))
             nk = (k + 63) // 64
-            best, best_ms = 1, float("inf")
+            best, best_ms = (1, 256), float("inf")
             results = {}
-            for s in CANDIDATES:
-                if s > max(1, nk):
-                    continue
-                check(lib.vkc_gemm_tune_set(prec, m, n, k, s))
-                ms = _time_gemm(gpu, A._dptr(), B._dptr(), Cm._buf.ptr, m, n, k, prec=prec)
-                results[s] = round(ms * 1e3, 1)
-                if ms < best_ms:
-                    best, best_ms = s, ms
-            check(lib.vkc_gemm_tune_set(prec, m, n, k, best))
-            entries.append([bucket(m), bucket(n), bucket(k), best])
+            for tile in TILES:
+                for s in CANDIDATES:
+                    if s > max(1, nk):
+                        continue
+                    check(lib.vkc_gemm_plan_set(prec, m, n, k, s, tile))
+                    ms = _time_gemm(gpu, A._dptr(), B._dptr(), Cm._buf.ptr, m, n, k, prec=prec)
+                    results[f"{tile}/{s}"] = round(ms * 1e3, 1)
+                    if ms < best_ms:
+                        best, best_ms = (s, tile), ms
+            check(lib.vkc_gemm_plan_set(prec, m, n, k, best[0], best[1]))
+            entries.append([bucket(m), bucket(n), bucket(k), best[0], best[1]])
             if verbose:
-                print(f"{name} M={m} N={n} K={k}: best splits {best} ({best_ms * 1e3:.1f} us)  {results}",
-                      flush=True)
+                print(f"{name} M={m} N={n} K={k}: best tile {best[1]} splits {best[0]} "
+                      f"({best_ms * 1e3:.1f} us)  {results}", flush=True)
         table[name] = entries
     table.update({"device": vk.GPU()._dev.name, "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
-                  "candidates": list(CANDIDATES)})
+                  "candidates": list(CANDIDATES), "tiles": list(TILES),
+                  "entry": "[log2 M, log2 N, log2 K, splits, tile width]"})
     return table
 
 

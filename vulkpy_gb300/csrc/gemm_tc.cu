@@ -48,17 +48,17 @@ namespace {
 // split mode (hi*hi + hi*lo + lo*hi): one accumulation per DRAIN K blocks;
 // the epilogue adds each into fp32 registers with round-to-nearest, so the
 // tensor pipe's truncating accumulation spans at most DRAIN*64 of K.
-constexpr int kBN2 = 256;          // columns of C per CTA tile
 constexpr int kEpiWarps = 8;
 constexpr int kThreadsP = 32 * (2 + kEpiWarps);
 constexpr int kGroupM = 8;         // cluster rows per raster group (L2 reuse)
 
 
-template <bool X3, int STAGES>
+// BN: columns of C per CTA tile (256 or 128; the autotuner picks per shape).
+template <bool X3, int BN, int STAGES>
 struct PCfg {
   static constexpr uint32_t kABytes = kBM * kBK * 2;             // 16 KB
-  static constexpr uint32_t kBHalf = 128 * kBK * 2;              // 16 KB
-  static constexpr uint32_t kBBytes = kBN2 * kBK * 2;            // 32 KB
+  static constexpr uint32_t kBHalf = (BN / 2) * kBK * 2;         // one CTA's half of the B tile
+  static constexpr uint32_t kBBytes = BN * kBK * 2;
   static constexpr uint32_t kStageBytes = (X3 ? 2u : 1u) * (kABytes + kBBytes);
   static constexpr uint32_t kBarOff = STAGES * kStageBytes;
   // full[S], empty[S], accf[2], acce[2], drain, then tmem slot + abort flag
@@ -70,6 +70,7 @@ struct PUnit {
   int m0, n0, kb0, nkb, z;
 };
 
+template <int BN>
 __device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int m_pairs, int n_blocks, int rank) {
   const int tile = u / splits, z = u - tile * splits;
   const int per_group = kGroupM * n_blocks;
@@ -79,7 +80,7 @@ __device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int
   const int mp = first + within % gsize, nb = within / gsize;
   PUnit p;
   p.m0 = (2 * mp + rank) * kBM;
-  p.n0 = nb * kBN2;
+  p.n0 = nb * BN;
   p.kb0 = z * kps;
   p.nkb = max(0, min(nk, p.kb0 + kps) - p.kb0);
   p.z = z;
@@ -129,14 +130,15 @@ __device__ __forceinline__ void store_row32(const float* acc, float* crow, const
   }
 }
 
-template <bool X3, int STAGES, int DRAIN>
+template <bool X3, int BN, int STAGES, int DRAIN>
 __global__ void __launch_bounds__(kThreadsP, 1)
 k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
            const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
            int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
            uint32_t* err, float* __restrict__ partial, int splits, int kps, int m_pairs, int n_blocks) {
-  using Cfg = PCfg<X3, STAGES>;
-  constexpr uint32_t kCols = 2 * kBN2;  // two accumulators: all 512 TMEM columns
+  using Cfg = PCfg<X3, BN, STAGES>;
+  constexpr uint32_t kCols = 2 * BN;  // two accumulators
+  constexpr int CW = BN / 2;          // columns per epilogue warp
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
@@ -198,8 +200,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     int it = 0;
     bool ok = true;
     for (int u = cluster; u < units && ok; u += nclusters) {
-      const PUnit p = unit_of(u, splits, kps, nk, m_pairs, n_blocks, rank);
-      const int nb_row = p.n0 + 128 * rank;
+      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_pairs, n_blocks, rank);
+      const int nb_row = p.n0 + (BN / 2) * rank;
       for (int kb = 0; kb < p.nkb; ++kb, ++it) {
         const int s = it % STAGES;
         if (*abort_flag || !mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1)) { ok = false; break; }
@@ -231,17 +233,17 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     constexpr uint32_t idesc = (1u << 4)            // D: fp32
                                | (1u << 7)          // A: bf16
                                | (1u << 10)         // B: bf16
-                               | ((uint32_t)(kBN2 >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+                               | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
     int it = 0, acc_it = 0;
     bool ok = true;
     for (int u = cluster; u < units && ok; u += nclusters) {
-      const PUnit p = unit_of(u, splits, kps, nk, m_pairs, n_blocks, rank);
+      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_pairs, n_blocks, rank);
       const int span = X3 ? DRAIN : p.nkb;  // K blocks per accumulation
       for (int g0 = 0; g0 < p.nkb && ok; g0 += span, ++acc_it) {
         const int b = acc_it & 1;
         if (*abort_flag || !mbar_wait(acce_bar(b), ((acc_it >> 1) & 1) ^ 1)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(b * kBN2);
+        const uint32_t d = tmem + (uint32_t)(b * BN);
         const int g1 = min(p.nkb, g0 + span);
         for (int kb = g0; kb < g1; ++kb, ++it) {
           const int s = it % STAGES;
@@ -278,18 +280,18 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     // fully unrolled 128-column epilogue the kernel spent most of a small
     // launch waiting on instruction fetch.
     const int q = warp & 3;          // TMEM lane quarter
-    const int h = (warp - 2) >> 2;   // column half of the 256-wide tile
+    const int h = (warp - 2) >> 2;   // column half of the tile
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
     int acc_it = 0;
     bool ok = true;
     for (int u = cluster; u < units && ok; u += nclusters) {
-      const PUnit p = unit_of(u, splits, kps, nk, m_pairs, n_blocks, rank);
+      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_pairs, n_blocks, rank);
       const int span = X3 ? DRAIN : p.nkb;
       const int ngroups = (p.nkb + span - 1) / span;
-      float acc[X3 ? 128 : 1];
+      float acc[X3 ? CW : 1];
       if (X3) {
 #pragma unroll
-        for (int j = 0; j < (X3 ? 128 : 1); ++j) acc[j] = 0.f;
+        for (int j = 0; j < (X3 ? CW : 1); ++j) acc[j] = 0.f;
       }
       int b = 0;
       for (int gi = 0; gi < ngroups; ++gi, ++acc_it) {
@@ -301,8 +303,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
           // the sums back into the buffer for the store loop below
           const bool last = gi == ngroups - 1;
 #pragma unroll
-          for (int c = 0; c < 4; c += 2) {
-            const uint32_t ta = tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32);
+          for (int c = 0; c < CW / 32; c += 2) {
+            const uint32_t ta = tmem + lane_addr + (uint32_t)(b * BN + h * CW + c * 32);
             uint32_t r0[32], r1[32];
             tmem_ld32_nw(ta, r0);
             tmem_ld32_nw(ta + 32, r1);
@@ -333,13 +335,13 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
       const bool raw_out = partial != nullptr;
       float* crow = raw_out ? partial + ((int64_t)p.z * M + row) * N : C + (int64_t)row * ldc;
 #pragma unroll 1
-      for (int c = 0; c < 4; c += 2) {
-        const uint32_t ta = tmem + lane_addr + (uint32_t)(b * kBN2 + h * 128 + c * 32);
+      for (int c = 0; c < CW / 32; c += 2) {
+        const uint32_t ta = tmem + lane_addr + (uint32_t)(b * BN + h * CW + c * 32);
         uint32_t r0[32], r1[32];
         tmem_ld32_nw(ta, r0);
         tmem_ld32_nw(ta + 32, r1);
         tmem_wait_ld();
-        const int col0 = p.n0 + h * 128 + c * 32;
+        const int col0 = p.n0 + h * CW + c * 32;
         if (row < M && col0 < N)
           store_row32(reinterpret_cast<const float*>(r0), crow, bias, col0, N, alpha, beta, act, raw_out);
         if (row < M && col0 + 32 < N)
@@ -545,9 +547,11 @@ int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t Kp, int bo
   return VKC_OK;
 }
 
-// ---- split-K tuning table: (precision, log2 buckets of M, N, K) -> splits.
-// Filled from the autotuner's table at import (vkc_gemm_tune_set); shapes
-// without an entry use the occupancy heuristic below.
+// ---- tuning table: (precision, log2 buckets of M, N, K) -> (tile width,
+// split count), filled from the autotuner's table at import (vkc_gemm_plan_set
+// / vkc_gemm_tune_set); shapes without an entry use the occupancy heuristic.
+// A value holds splits in the low 16 bits and the tile width (128 or 256;
+// 0 = 256) above them.
 std::mutex g_tune_mu;
 std::map<uint64_t, int> g_tune;
 
@@ -569,13 +573,28 @@ int heuristic_splits(vkc_device_t dev, int64_t tiles, int nk) {
   return splits;
 }
 
-int choose_splits(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_t K, int64_t tiles, int nk) {
+struct TcPlan {
+  int bn;      // columns of C per CTA tile
+  int splits;  // K ranges
+};
+
+// CTA tiles (128 x bn) of an M x N problem, counting the idle partner of an
+// odd last row of tiles (the 2-CTA clusters pair tile rows).
+inline int64_t cta_tiles(int64_t M, int64_t N, int bn) {
+  return 2 * (((M + kBM - 1) / kBM + 1) / 2) * ((N + bn - 1) / bn);
+}
+
+TcPlan choose_plan(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_t K) {
+  const int nk = (int)std::max<int64_t>(1, (K + kBK - 1) / kBK);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(tune_key(precision, bucket(M), bucket(N), bucket(K)));
-    if (it != g_tune.end()) return std::max(1, std::min(it->second, std::max(1, nk)));
+    if (it != g_tune.end()) {
+      const int bn = (it->second >> 16) == 128 ? 128 : 256;
+      return TcPlan{bn, std::max(1, std::min(it->second & 0xffff, nk))};
+    }
   }
-  return heuristic_splits(dev, tiles, nk);
+  return TcPlan{256, heuristic_splits(dev, cta_tiles(M, N, 256), nk)};
 }
 
 // C = act(alpha * sum_z partial[z] + beta * C + bias), z in order.
@@ -683,12 +702,12 @@ int max_clusters(vkc_device_t dev, Kern kern, uint32_t smem) {
   return n;
 }
 
-template <bool X3, int STAGES, int DRAIN>
+template <bool X3, int BN, int STAGES, int DRAIN>
 int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
                const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C,
-               int64_t ldc, const GemmEpilogue& epi) {
-  using Cfg = PCfg<X3, STAGES>;
-  auto kern = k_gemm_tcp<X3, STAGES, DRAIN>;
+               int64_t ldc, const GemmEpilogue& epi, int splits) {
+  using Cfg = PCfg<X3, BN, STAGES>;
+  auto kern = k_gemm_tcp<X3, BN, STAGES, DRAIN>;
   static bool attr_set = false;
   if (!attr_set) {
     VKC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
@@ -696,12 +715,10 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
   }
   const int64_t m_blocks = (M + kBM - 1) / kBM;
   const int m_pairs = (int)((m_blocks + 1) / 2);
-  const int n_blocks = (int)((N + kBN2 - 1) / kBN2);
+  const int n_blocks = (int)((N + BN - 1) / BN);
   const int64_t tiles = (int64_t)m_pairs * n_blocks;
   const int nk = (int)((K + kBK - 1) / kBK);
-  // Split K when the 256 x 256 units alone would leave most SMs idle (tuning
-  // table first, then the occupancy heuristic); no empty split.
-  int splits = choose_splits(dev, X3 ? VKC_MM_BF16X3 : VKC_MM_BF16, M, N, K, 2 * tiles, nk);
+  // no empty split
   const int kps = (nk + splits - 1) / splits;
   splits = (nk + kps - 1) / kps;
   float* partial = nullptr;
@@ -736,21 +753,31 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
 
 }  // namespace vkc
 
-VKC_EXPORT int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k, int splits) {
+VKC_EXPORT int vkc_gemm_plan_set(int precision, int64_t m, int64_t n, int64_t k, int splits, int tile_n) {
   VKC_REQUIRE(splits >= 0 && splits <= 64, "splits out of range");
+  VKC_REQUIRE(tile_n == 128 || tile_n == 256, "tile width must be 128 or 256");
   std::lock_guard<std::mutex> lk(vkc::g_tune_mu);
   auto key = vkc::tune_key(precision, vkc::bucket(m), vkc::bucket(n), vkc::bucket(k));
   if (splits == 0) vkc::g_tune.erase(key);
-  else vkc::g_tune[key] = splits;
+  else vkc::g_tune[key] = splits | (tile_n << 16);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k, int splits) {
+  return vkc_gemm_plan_set(precision, m, n, k, splits, 256);
+}
+
+VKC_EXPORT int vkc_gemm_plan_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits,
+                                 int* tile_n) {
+  VKC_REQUIRE(dev && splits, "NULL argument");
+  const vkc::TcPlan p = vkc::choose_plan(dev, precision, m, n, k);
+  *splits = p.splits;
+  if (tile_n) *tile_n = p.bn;
   return VKC_OK;
 }
 
 VKC_EXPORT int vkc_gemm_tune_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits) {
-  VKC_REQUIRE(dev && splits, "NULL argument");
-  const int64_t tiles = 2 * (((m + 127) / 128 + 1) / 2) * ((n + 255) / 256);  // CTA tiles, 128 x 256
-  const int nk = (int)((k + 63) / 64);
-  *splits = vkc::choose_splits(dev, precision, m, n, k, tiles, nk);
-  return VKC_OK;
+  return vkc_gemm_plan_get(dev, precision, m, n, k, splits, nullptr);
 }
 
 VKC_EXPORT int vkc_gemm_tune_clear(void) {
@@ -786,16 +813,24 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   // op(B)(k,n): tb ? B[n*ldb + k] : B[k*ldb + n]  -> (n,k) K contiguous iff tb
   r = split_operand(dev, A, M, K, lda, !ta, a_hi, a_lo, Kp);
   if (r == VKC_OK) r = split_operand(dev, B, N, K, ldb, tb, b_hi, b_lo, Kp);
-  // every box is 128 rows x 64 K: a CTA's op(A) tile or one half of the
-  // 256-row op(B) tile
+  // boxes are 64 K wide: 128 rows for a CTA's op(A) tile, bn/2 rows for
+  // one CTA's half of the op(B) tile
+  const TcPlan plan = choose_plan(dev, precision, M, N, K);
   CUtensorMap ma, mb, malo, mblo;
   if (r == VKC_OK) r = make_map(&ma, a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, 128);
+  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, plan.bn / 2);
   if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, 128);
+  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, plan.bn / 2);
   if (r == VKC_OK) {
-    if (x3) r = launch_tcp<true, 2, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
-    else r = launch_tcp<false, 4, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi);
+    // stages fill ~192 KB of shared memory
+    if (x3 && plan.bn == 256)
+      r = launch_tcp<true, 256, 2, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
+    else if (x3)
+      r = launch_tcp<true, 128, 3, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
+    else if (plan.bn == 256)
+      r = launch_tcp<false, 256, 4, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
+    else
+      r = launch_tcp<false, 128, 6, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
   }
   scratch_free(dev, scratch);
   return r;

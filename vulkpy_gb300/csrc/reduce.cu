@@ -381,13 +381,14 @@ k_cols(const float* a, size_t prev, size_t axis, size_t post, int splits, float*
   const float* base = a + i * axis * post + j;
   size_t k = k0;
   if constexpr (VW == 4) {
-    // four rows per iteration: independent loads in flight, applied in order
-    for (; k + 3 < k1; k += 4) {
-      float4 v[4];
+    // eight rows per iteration: 128 bytes of independent loads in flight per
+    // thread (four rows left HBM ~30% idle), applied in row order
+    for (; k + 7 < k1; k += 8) {
+      float4 v[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = *reinterpret_cast<const float4*>(base + (k + u) * post);
+      for (int u = 0; u < 8; ++u) v[u] = __ldcs(reinterpret_cast<const float4*>(base + (k + u) * post));
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         acc[0].push(v[u].x); acc[1].push(v[u].y); acc[2].push(v[u].z); acc[3].push(v[u].w);
       }
     }
