@@ -385,9 +385,13 @@ int vkc_adam_update(vkc_device_t dev, float* value, const float* grad, float* m,
                     size_t n, double lr, double beta1, double beta2, double eps,
                     double beta1t, double beta2t);
 /* Adam with the running powers beta1^t, beta2^t kept on the device
- * (`powers` = double[2], start at {1, 1}); the call multiplies them by
- * beta1, beta2 first, exactly as AdamState.grad2diff does on the host, so a
- * captured step can be replayed.  Same result as vkc_adam_update. */
+ * (`powers` = double[3], start at {1, 1, 0}; the third slot is the kernel's
+ * completion counter and is back at 0 after every call).  The update uses
+ * beta1^t * beta1 and beta2^t * beta2 (in double), exactly as
+ * AdamState.grad2diff advances them on the host, and the last block of the
+ * same launch stores the advanced powers, so a captured step can be
+ * replayed.  Same result as vkc_adam_update.  Calls on one `powers` buffer
+ * must not overlap on the GPU. */
 int vkc_adam_update_dev(vkc_device_t dev, float* value, const float* grad, float* m, float* v,
                         size_t n, double lr, double beta1, double beta2, double eps, double* powers);
 /* dx = dy * f'(y) from the activation output y: ReLU dy * max(sign(y), 0)

@@ -397,13 +397,14 @@ __global__ void k_split_kmajor(const float* __restrict__ src, int64_t R, int64_t
 
 // The same with 8 elements per thread: 2 x float4 in, one 16-byte store per
 // output (ld % 4 == 0, 16-byte aligned source, Kp % 8 == 0); the chunk that
-// straddles K is read element by element, chunks past K are zero.
-__global__ void __launch_bounds__(256)
-k_split_kmajor8(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
-                __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+// straddles K is read element by element, chunks past K are zero.  Blocks
+// `blk` of `nblk` stride over the chunks.
+__device__ __forceinline__ void split_kmajor8_body(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
+                                                   __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                                   int64_t Kp, int64_t blk, int64_t nblk) {
   const int64_t per_row = Kp / 8, total = R * per_row;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+  const int64_t stride = nblk * blockDim.x;
+  for (int64_t i = blk * blockDim.x + threadIdx.x; i < total; i += stride) {
     const int64_t r = i / per_row, k = (i - r * per_row) * 8;
     float x[8];
     if (k + 8 <= K) {
@@ -422,17 +423,23 @@ k_split_kmajor8(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
   }
 }
 
+__global__ void __launch_bounds__(256)
+k_split_kmajor8(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
+                __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+  split_kmajor8_body(src, R, K, ld, hi, lo, Kp, blockIdx.x, gridDim.x);
+}
+
 // K is the row index of the source (src[k*ld + r]): 64 (k) x 64 (r) tiles
 // through shared memory.  Reads: each thread one float4 of a k row (16 rows
 // of 256 bytes per pass); writes: each thread 8 consecutive k of one r as a
 // 16-byte store (8 rows of 128 bytes per pass).  Requires ld % 4 == 0 and a
 // 16-byte aligned source; R need not be a multiple of 4 (the tail of a
-// row is read element by element).
-__global__ void __launch_bounds__(256)
-k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
-                  __nv_bfloat16* __restrict__ lo, int64_t Kp) {
-  __shared__ float tile[64][65];
-  const int64_t r0 = (int64_t)blockIdx.x * 64, k0 = (int64_t)blockIdx.y * 64;
+// row is read element by element).  256 threads; tile (bx, by) covers rows
+// r in [64 bx, 64 bx + 64), k in [64 by, 64 by + 64).
+__device__ __forceinline__ void split_transpose_body(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
+                                                     __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                                     int64_t Kp, int64_t bx, int64_t by, float (*tile)[65]) {
+  const int64_t r0 = bx * 64, k0 = by * 64;
   const int t = threadIdx.x;
   {
     const int c4 = (t & 15) * 4, kr = t >> 4;  // 16 float4 per 64-wide row, 16 rows per pass
@@ -469,6 +476,37 @@ k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t l
       if (lo) *reinterpret_cast<uint4*>(lo + r * Kp + k) = *reinterpret_cast<const uint4*>(l);
     }
   }
+}
+
+__global__ void __launch_bounds__(256)
+k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
+                  __nv_bfloat16* __restrict__ lo, int64_t Kp) {
+  __shared__ float tile[64][65];
+  split_transpose_body(src, R, K, ld, hi, lo, Kp, blockIdx.x, blockIdx.y, tile);
+}
+
+// Both operands of a GEMM in one launch (two launches cost more than the
+// conversion itself for the small GEMMs of an MLP step): blocks [0, a.blocks)
+// convert op(A), the rest op(B).
+struct SplitJob {
+  const float* src;
+  int64_t R, K, ld, Kp;
+  __nv_bfloat16* hi;
+  __nv_bfloat16* lo;
+  int64_t tiles_x;  // transpose: tiles along R; 0: K contiguous (8 per thread)
+  int64_t blocks;
+};
+
+__global__ void __launch_bounds__(256) k_split_pair(const __grid_constant__ SplitJob a,
+                                                    const __grid_constant__ SplitJob b) {
+  __shared__ float tile[64][65];
+  const bool first = blockIdx.x < a.blocks;
+  const SplitJob& j = first ? a : b;
+  const int64_t blk = first ? (int64_t)blockIdx.x : (int64_t)blockIdx.x - a.blocks;
+  if (j.tiles_x == 0)
+    split_kmajor8_body(j.src, j.R, j.K, j.ld, j.hi, j.lo, j.Kp, blk, j.blocks);
+  else
+    split_transpose_body(j.src, j.R, j.K, j.ld, j.hi, j.lo, j.Kp, blk % j.tiles_x, blk / j.tiles_x, tile);
 }
 
 // Fallback for unaligned sources: 32 x 32 tiles, one element per access.
@@ -515,6 +553,35 @@ int split_operand(vkc_device_t dev, const float* src, int64_t R, int64_t K, int6
     k_split_transpose1<<<grid, dim3(32, 8), 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
   }
   return check_launch("split_operand");
+}
+
+// Both operands: one k_split_pair launch when both sources allow the vector
+// paths, else one launch each.
+int split_operands(vkc_device_t dev, const float* A, int64_t M, int64_t lda, bool a_kcontig, __nv_bfloat16* a_hi,
+                   __nv_bfloat16* a_lo, const float* B, int64_t N, int64_t ldb, bool b_kcontig,
+                   __nv_bfloat16* b_hi, __nv_bfloat16* b_lo, int64_t K, int64_t Kp) {
+  auto aligned = [](const float* p, int64_t ld) { return ld % 4 == 0 && ((uintptr_t)p & 15u) == 0; };
+  if (!aligned(A, lda) || !aligned(B, ldb) || (Kp + 63) / 64 > 65535) {
+    int r = split_operand(dev, A, M, K, lda, a_kcontig, a_hi, a_lo, Kp);
+    if (r == VKC_OK) r = split_operand(dev, B, N, K, ldb, b_kcontig, b_hi, b_lo, Kp);
+    return r;
+  }
+  const int64_t cap = (int64_t)dev->sm_count * resident_blocks((const void*)k_split_pair, 256);
+  auto job = [&](const float* src, int64_t R, int64_t ld, bool kcontig, __nv_bfloat16* hi, __nv_bfloat16* lo) {
+    SplitJob j{src, R, K, ld, Kp, hi, lo, 0, 0};
+    if (kcontig) {
+      j.blocks = std::max<int64_t>(1, std::min<int64_t>((R * (Kp / 8) + 255) / 256, cap));
+    } else {
+      j.tiles_x = (R + 63) / 64;
+      j.blocks = j.tiles_x * ((Kp + 63) / 64);
+    }
+    return j;
+  };
+  const SplitJob ja = job(A, M, lda, a_kcontig, a_hi, a_lo), jb = job(B, N, ldb, b_kcontig, b_hi, b_lo);
+  const int64_t grid = ja.blocks + jb.blocks;
+  if (grid > 0x7fffffff) return set_error(VKC_ERR_INVALID, "matmul: operands too large for the pre-pass grid");
+  k_split_pair<<<(unsigned)grid, 256, 0, dev->stream>>>(ja, jb);
+  return check_launch("split_operands");
 }
 
 // ------------------------------------------------------------ host side
@@ -811,8 +878,7 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   __nv_bfloat16* b_lo = x3 ? a_lo + a_elems : nullptr;
   // op(A)(m,k): ta ? A[k*lda + m] : A[m*lda + k]  -> K contiguous iff !ta
   // op(B)(k,n): tb ? B[n*ldb + k] : B[k*ldb + n]  -> (n,k) K contiguous iff tb
-  r = split_operand(dev, A, M, K, lda, !ta, a_hi, a_lo, Kp);
-  if (r == VKC_OK) r = split_operand(dev, B, N, K, ldb, tb, b_hi, b_lo, Kp);
+  r = split_operands(dev, A, M, lda, !ta, a_hi, a_lo, B, N, ldb, tb, b_hi, b_lo, K, Kp);
   // boxes are 64 K wide: 128 rows for a CTA's op(A) tile, bn/2 rows for
   // one CTA's half of the op(B) tile
   const TcPlan plan = choose_plan(dev, precision, M, N, K);

@@ -139,15 +139,15 @@ k_adagrad(float* value, const float* grad, float* h, size_t n, float nlr, float 
 
 // Running powers for the device-resident Adam variant: p *= beta, in double
 // exactly like the Python floats of AdamState (optimizers.py:241-242).
-__global__ void k_adam_powers(double* p, double beta1, double beta2) {
-  p[0] *= beta1;
-  p[1] *= beta2;
-}
-
+// Adam step with the running powers on the device: every thread advances
+// beta^t from the stored value (the same double product on every thread);
+// the last block to finish stores the advanced powers and resets the
+// completion counter in powers[2], so one launch both uses and advances them.
 __global__ void __launch_bounds__(kThreads)
 k_adam_dev(float* value, const float* grad, float* m, float* v, size_t n, float b1, float c1, float b2, float c2,
-           const double* powers, float eps, float nlr) {
-  const float d1 = (float)(1.0 - powers[0]), d2 = (float)(1.0 - powers[1]);
+           double* powers, double beta1, double beta2, float eps, float nlr) {
+  const double p1 = powers[0] * beta1, p2 = powers[1] * beta2;
+  const float d1 = (float)(1.0 - p1), d2 = (float)(1.0 - p2);
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const float g = grad[i];
@@ -160,6 +160,17 @@ k_adam_dev(float* value, const float* grad, float* m, float* v, size_t n, float 
     mhat = __fmul_rn(mhat, nlr);
     mhat = __fdiv_rn(mhat, vhat);
     value[i] = __fadd_rn(value[i], mhat);
+  }
+  __syncthreads();  // this block has read powers[0..1]
+  if (threadIdx.x == 0) {
+    unsigned int* done = reinterpret_cast<unsigned int*>(powers + 2);
+    __threadfence();
+    if (atomicAdd(done, 1u) == gridDim.x - 1) {  // every block has read the old powers
+      powers[0] = p1;
+      powers[1] = p2;
+      *done = 0u;
+      __threadfence();
+    }
   }
 }
 
@@ -193,13 +204,10 @@ VKC_EXPORT int vkc_adam_update_dev(vkc_device_t dev, float* value, const float* 
                                    double lr, double beta1, double beta2, double eps, double* powers) {
   VKC_BIND(dev);
   VKC_REQUIRE(value && grad && m && v && powers, "NULL buffer");
-  k_adam_powers<<<1, 1, 0, dev->stream>>>(powers, beta1, beta2);
-  int r = vkc::check_launch("adam_powers");
-  if (r != VKC_OK || n == 0) return r;
   unsigned grid = vkc::wave_grid(dev, k_adam_dev, n, kThreads);
   k_adam_dev<<<grid, kThreads, 0, dev->stream>>>(value, grad, m, v, n, (float)beta1, (float)(1.0 - beta1),
-                                                 (float)beta2, (float)(1.0 - beta2), powers, (float)eps,
-                                                 (float)(-lr));
+                                                 (float)beta2, (float)(1.0 - beta2), powers, beta1, beta2,
+                                                 (float)eps, (float)(-lr));
   return vkc::check_launch("adam_dev");
 }
 

@@ -91,9 +91,10 @@ class AdamState(OptimizerState):
         self.v: Array = zeros(self.opt.gpu, shape=shape)
         self.beta1t: float = 1.0
         self.beta2t: float = 1.0
-        # the same running powers on the device (two doubles), advanced by the
-        # update kernel itself so that a captured training step can be replayed
-        self._powers = U32Array(self.opt.gpu, data=np.array([1.0, 1.0], dtype=np.float64).view(np.uint32))
+        # the same running powers on the device (two doubles and the update
+        # kernel's completion counter), advanced by the update kernel itself
+        # so that a captured training step can be replayed
+        self._powers = U32Array(self.opt.gpu, data=np.array([1.0, 1.0, 0.0], dtype=np.float64).view(np.uint32))
 
     def grad2diff(self, grad: Array) -> Array:
         diff = zeros(self.opt.gpu, shape=grad.shape)
