@@ -297,6 +297,17 @@ int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* d
 /* value[i] += (-lr) * grad[i] for every tensor (optimizers.py:24-60). */
 int vkc_sgd_update_grouped(vkc_device_t dev, float* const* value, const float* const* grad, const int64_t* n,
                            double lr, int count);
+/* Adam for `count` tensors with shared hyperparameters in one launch, each
+ * with its own moments and running powers (double[3] as for
+ * vkc_adam_update_dev); per tensor the result equals vkc_adam_update_dev's.
+ * Replaces one AdamState.grad2diff + Parameter.update per tensor
+ * (optimizers.py:221-253, parameters.py:88-95). */
+int vkc_adam_update_grouped(vkc_device_t dev, float* const* value, const float* const* grad,
+                            float* const* m, float* const* v, double* const* powers, const int64_t* n,
+                            int count, double lr, double beta1, double beta2, double eps);
+/* dst[i][0..n[i]) = v for every tensor: Sequence's zero_grad of every
+ * parameter in one launch (parameters.py:81-86, models.py:47-49). */
+int vkc_fill_f32_grouped(vkc_device_t dev, float* const* dst, const int64_t* n, float v, int count);
 /* MSELoss with reduce="mean" for many models (losses.py:252-320 with
  * ReduceLoss 40-92): dx[i] = ((x - y) * 2) * float32(1/batch) (when dx is
  * not NULL) and loss[i] = mean over rows of sum over columns of (y - x)^2

@@ -211,3 +211,47 @@ def test_branches_in_a_graph_match_sequential_eager(gpu, vk):
     for a, b in zip(ref, eager):
         for pa, pb in zip(_params(a), _params(b)):
             np.testing.assert_array_equal(pa, pb)
+
+
+@pytest.mark.parametrize("optname", ["adam", "sgd"])
+def test_grouped_parameter_update_matches_per_parameter(gpu, vk, optname):
+    """A Sequence whose parameters share one optimizer zeroes every gradient
+    and updates every parameter in one launch each; a copy whose layers have
+    their own optimizer objects (same hyperparameters) takes the
+    per-parameter path.  Parameters, moments and the device-side Adam powers
+    match bit for bit, eager and replayed from a captured step."""
+    nn = vk.nn
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal((24, 12)).astype(f32)
+    Y = np.eye(3, dtype=f32)[rng.integers(0, 3, 24)]
+
+    def make(shared):
+        mk = (lambda: nn.Adam(gpu, lr=1e-2)) if optname == "adam" else (lambda: nn.SGD(lr=1e-2))
+        o = mk()
+        opts = [o if shared else mk() for _ in range(4)]
+        return nn.Sequence([
+            nn.Dense(gpu, 12, 16, w_opt=opts[0], b_opt=opts[1], w_init=nn.HeNormal(gpu, 12, seed=3)),
+            nn.ReLU(),
+            nn.Dense(gpu, 16, 3, w_opt=opts[2], b_opt=opts[3], w_init=nn.HeNormal(gpu, 16, seed=4)),
+        ], nn.SoftmaxCrossEntropyLoss())
+
+    per, grouped, graphed = make(False), make(True), make(True)
+    assert per._update_grouped(per._params()) is False   # separate optimizers: per-parameter path
+    x, y = vk.Array(gpu, data=X), vk.Array(gpu, data=Y)
+    for _ in range(3):
+        per.train(x, y)
+        grouped.train(x, y)
+    graphed.train(x, y)
+    step = graphed.compile(x, y)
+    step()
+    step()
+    for a, b, c in zip(_params(per), _params(grouped), _params(graphed)):
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(a, c)
+    if optname == "adam":
+        for La, Lb in ((per.L[0], grouped.L[0]), (per.L[2], grouped.L[2])):
+            for pa, pb in ((La.w, Lb.w), (La.b, Lb.b)):
+                np.testing.assert_array_equal(np.asarray(pa.opt_state.m), np.asarray(pb.opt_state.m))
+                np.testing.assert_array_equal(np.asarray(pa.opt_state.v), np.asarray(pb.opt_state.v))
+                np.testing.assert_array_equal(np.asarray(pa.opt_state._powers), np.asarray(pb.opt_state._powers))
+                assert pa.opt_state.beta1t == pb.opt_state.beta1t

@@ -101,6 +101,8 @@ _SIGS = {
     "vkc_gemm_grouped": ([vp, i32, C.POINTER(GemmProblem), i32], i32),
     "vkc_colsum_grouped": ([vp, pvp, pvp, pi64, pi64, i32, i32], i32),
     "vkc_sgd_update_grouped": ([vp, pvp, pvp, pi64, f64, i32], i32),
+    "vkc_adam_update_grouped": ([vp, pvp, pvp, pvp, pvp, pvp, pi64, i32, f64, f64, f64, f64], i32),
+    "vkc_fill_f32_grouped": ([vp, pvp, pi64, f32, i32], i32),
     "vkc_mse_grouped": ([vp, pvp, pvp, pvp, pi64, pi64, vp, i32], i32),
     "vkc_gather": ([vp, vp, sz, vp, sz, vp], i32),
     "vkc_gather_axis": ([vp, vp, sz, sz, sz, vp, sz, vp], i32),

@@ -498,6 +498,75 @@ __global__ void __launch_bounds__(256) k_sgd_grouped(const __grid_constant__ Vec
   }
 }
 
+// dst[i] = v for every tensor (zero_grad of every parameter in one launch).
+__global__ void __launch_bounds__(256) k_fill_grouped(const __grid_constant__ VecTable tab) {
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    const VecItem& I = tab.it[find_vec(tab, t)];
+    const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
+    const int64_t i1 = min(i0 + kVecChunk, I.n);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) I.value[i] = I.scale;
+  }
+}
+
+// Adam for many tensors in one launch: each tensor's arithmetic is the
+// single-tensor kernel's (k_adam_dev in nn.cu), and each keeps its own
+// running powers; the last chunk of a tensor to finish stores its advanced
+// powers (every chunk has read the old ones by then) and resets the counter.
+struct AdamItem {
+  float* value;
+  const float* grad;
+  float* m;
+  float* v;
+  double* powers;  // beta1^t, beta2^t, completion counter
+  int64_t n;
+  int block0, chunks;
+};
+struct AdamTable {
+  int count, total;
+  float b1, c1, b2, c2, eps, nlr;
+  double beta1, beta2;
+  AdamItem it[kMaxGroup];
+};
+
+__global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ AdamTable tab) {
+  for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
+    int lo = 0, hi = tab.count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab.it[mid].block0 <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const AdamItem& I = tab.it[lo];
+    const double p1 = I.powers[0] * tab.beta1, p2 = I.powers[1] * tab.beta2;
+    const float d1 = (float)(1.0 - p1), d2 = (float)(1.0 - p2);
+    const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
+    const int64_t i1 = min(i0 + kVecChunk, I.n);
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) {
+      const float gi = I.grad[i];
+      float mi = __fadd_rn(__fmul_rn(I.m[i], tab.b1), __fmul_rn(tab.c1, gi));
+      float vi = __fadd_rn(__fmul_rn(I.v[i], tab.b2), __fmul_rn(tab.c2, __fmul_rn(gi, gi)));
+      I.m[i] = mi;
+      I.v[i] = vi;
+      float mhat = __fdiv_rn(mi, d1);
+      float vhat = __fadd_rn(__fsqrt_rn(__fdiv_rn(vi, d2)), tab.eps);
+      mhat = __fmul_rn(mhat, tab.nlr);
+      mhat = __fdiv_rn(mhat, vhat);
+      I.value[i] = __fadd_rn(I.value[i], mhat);
+    }
+    __syncthreads();  // this chunk has read the powers
+    if (threadIdx.x == 0) {
+      unsigned int* done = reinterpret_cast<unsigned int*>(I.powers + 2);
+      __threadfence();
+      if (atomicAdd(done, 1u) == (unsigned)I.chunks - 1) {
+        I.powers[0] = p1;
+        I.powers[1] = p2;
+        *done = 0u;
+        __threadfence();
+      }
+    }
+  }
+}
+
 // MSE gradient of the mean-reduced loss: ((x - y) * 2) * float32(1/batch),
 // the three float32 operations of MSELoss.backward and ReduceLoss.grad.
 __global__ void __launch_bounds__(256) k_mse_grad_grouped(const __grid_constant__ VecTable tab) {
@@ -790,6 +859,9 @@ int vec_launch(vkc_device_t dev, int kind, float* const* value, const float* con
     if (tab.count == 0) continue;
     if (kind == 0) {
       k_sgd_grouped<<<(unsigned)std::min<int>(std::max(total, 1), dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
+    } else if (kind == 3) {
+      if (total == 0) continue;
+      k_fill_grouped<<<(unsigned)std::min<int>(total, dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
     } else if (kind == 1) {
       k_mse_grad_grouped<<<(unsigned)std::min<int>(std::max(total, 1), dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
     } else {
@@ -811,6 +883,51 @@ VKC_EXPORT int vkc_sgd_update_grouped(vkc_device_t dev, float* const* value, con
   for (int i = 0; i < count; ++i) VKC_REQUIRE(n[i] == 0 || (value[i] && grad[i]), "NULL buffer");
   std::vector<float> scale((size_t)count, (float)(-lr));
   return vec_launch(dev, 0, value, grad, nullptr, n, nullptr, scale.data(), count, nullptr);
+}
+
+VKC_EXPORT int vkc_fill_f32_grouped(vkc_device_t dev, float* const* dst, const int64_t* n, float v, int count) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(count >= 0, "negative item count");
+  if (count == 0) return VKC_OK;
+  VKC_REQUIRE(dst && n, "NULL argument");
+  for (int i = 0; i < count; ++i) VKC_REQUIRE(n[i] == 0 || dst[i], "NULL buffer");
+  std::vector<float> scale((size_t)count, v);
+  return vec_launch(dev, 3, dst, const_cast<const float* const*>(dst), nullptr, n, nullptr, scale.data(), count,
+                    nullptr);
+}
+
+VKC_EXPORT int vkc_adam_update_grouped(vkc_device_t dev, float* const* value, const float* const* grad,
+                                       float* const* m, float* const* v, double* const* powers, const int64_t* n,
+                                       int count, double lr, double beta1, double beta2, double eps) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(count >= 0, "negative item count");
+  if (count == 0) return VKC_OK;
+  VKC_REQUIRE(value && grad && m && v && powers && n, "NULL argument");
+  for (int s = 0; s < count; s += kMaxGroup) {
+    AdamTable tab{};
+    tab.b1 = (float)beta1;
+    tab.c1 = (float)(1.0 - beta1);
+    tab.b2 = (float)beta2;
+    tab.c2 = (float)(1.0 - beta2);
+    tab.eps = (float)eps;
+    tab.nlr = (float)(-lr);
+    tab.beta1 = beta1;
+    tab.beta2 = beta2;
+    int total = 0;
+    for (int i = s; i < std::min(count, s + kMaxGroup); ++i) {
+      VKC_REQUIRE(n[i] >= 0, "negative size");
+      VKC_REQUIRE(powers[i] && (n[i] == 0 || (value[i] && grad[i] && m[i] && v[i])), "NULL buffer");
+      AdamItem& I = tab.it[tab.count++];
+      I = AdamItem{value[i], grad[i], m[i], v[i], powers[i], n[i], total,
+                   (int)std::max<int64_t>(1, (n[i] + kVecChunk - 1) / kVecChunk)};
+      total += I.chunks;  // an empty tensor still gets one chunk: its powers advance
+    }
+    tab.total = total;
+    k_adam_grouped<<<(unsigned)std::min<int>(total, dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
+    int r = check_launch("adam_grouped");
+    if (r != VKC_OK) return r;
+  }
+  return VKC_OK;
 }
 
 VKC_EXPORT int vkc_mse_grouped(vkc_device_t dev, const float* const* x, const float* const* y, float* const* dx,

@@ -3,10 +3,14 @@ from __future__ import annotations
 
 from typing import Iterable, Optional, Tuple, Union
 
+import ctypes as C
+
 from ..vkarray import Array
 from ..graph import Graph
+from .._lib import lib, check
 from .core import Module, Loss
 from .layers import Dense, ReLU, Sigmoid
+from .optimizers import AdamState, SGDState
 
 __all__ = ["Sequence", "CompiledStep"]
 
@@ -61,17 +65,76 @@ class Sequence:
             else:
                 dx = layer.backward(dx)
 
-    def _zero_grad(self):
+    def _params(self):
+        """The trainable Parameters of the Dense layers, or None when another
+        layer type (which may hold its own parameters) is present."""
+        ps = []
         for _L in self.L:
-            _L.zero_grad()
+            if type(_L) is Dense:
+                ps.extend(p for p in (_L.w, _L.b) if p.grad is not None)
+            elif not isinstance(_L, (ReLU, Sigmoid)) and (hasattr(_L, "w") or hasattr(_L, "b")):
+                return None
+        return ps
+
+    def _zero_grad(self):
+        # every gradient in one launch (the same zeros as Parameter.zero_grad)
+        ps = self._params()
+        if not ps:
+            for _L in self.L:
+                _L.zero_grad()
+            return
+        for _L in self.L:
+            if type(_L) is not Dense:
+                _L.zero_grad()
+        gpu = ps[0].grad._gpu
+        n = len(ps)
+        check(lib.vkc_fill_f32_grouped(gpu._dev.h, (C.c_void_p * n)(*[p.grad._dptr() for p in ps]),
+                                       (C.c_int64 * n)(*[p.grad._size for p in ps]), 0.0, n))
+        for p in ps:
+            p.grad._written()
 
     def _update(self):
-        for _L in self.L:
-            if self.apply_regularizers:
+        if self.apply_regularizers:
+            for _L in self.L:
                 for p in (getattr(_L, "w", None), getattr(_L, "b", None)):
                     if p is not None:
                         p.regular_grad()
+        ps = self._params()
+        if ps and self._update_grouped(ps):
+            return
+        for _L in self.L:
             _L.update()
+
+    def _update_grouped(self, ps) -> bool:
+        """One launch for every parameter when they share one Adam or one SGD
+        optimizer (per tensor the same arithmetic as Parameter.update)."""
+        st = [p.opt_state for p in ps]
+        opt = st[0].opt
+        if any(s.opt is not opt for s in st):
+            return False
+        gpu = ps[0].value._gpu
+        n = len(ps)
+        vals = (C.c_void_p * n)(*[p.value._dptr() for p in ps])
+        grads = (C.c_void_p * n)(*[p.grad._dptr() for p in ps])
+        sizes = (C.c_int64 * n)(*[p.value._size for p in ps])
+        if all(type(s) is AdamState for s in st):
+            check(lib.vkc_adam_update_grouped(
+                gpu._dev.h, vals, grads, (C.c_void_p * n)(*[s.m._dptr() for s in st]),
+                (C.c_void_p * n)(*[s.v._dptr() for s in st]), (C.c_void_p * n)(*[s._powers._dptr() for s in st]),
+                sizes, n, float(opt.lr), float(opt.beta1), float(opt.beta2), float(opt.eps)))
+            for s in st:
+                s.beta1t *= opt.beta1
+                s.beta2t *= opt.beta2
+                s._powers._written()
+                s.m._written()
+                s.v._written()
+        elif all(type(s) is SGDState for s in st):
+            check(lib.vkc_sgd_update_grouped(gpu._dev.h, vals, grads, sizes, float(opt.lr), n))
+        else:
+            return False
+        for p in ps:
+            p.value._written()
+        return True
 
     def train(self, x: Array, y: Array) -> Tuple[Array, Array]:
         """One step: forward, loss, zero_grad, backward, update (models.py:55-78)."""
