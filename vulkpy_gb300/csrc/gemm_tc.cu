@@ -15,6 +15,7 @@
 // word, drains what it issued and returns.
 #include "gemm_tc.cuh"
 #include "tc_ptx.cuh"
+#include "tc_epilogue.cuh"
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -63,7 +64,8 @@ struct PCfg {
   static constexpr uint32_t kBarOff = STAGES * kStageBytes;
   // full[S], empty[S], accf[2], acce[2], drain, then tmem slot + abort flag
   static constexpr uint32_t kSlotOff = kBarOff + 8u * (2 * STAGES + 5);
-  static constexpr uint32_t kSmem = kSlotOff + 16 + 1024 /*alignment slack*/;
+  static constexpr uint32_t kEpiOff = (kSlotOff + 16 + 127) / 128 * 128;  // per-warp epilogue stages
+  static constexpr uint32_t kSmem = kEpiOff + kEpiWarps * kEpiStageBytes + 1024 /*alignment slack*/;
 };
 
 struct PUnit {
@@ -85,49 +87,6 @@ __device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int
   p.nkb = max(0, min(nk, p.kb0 + kps) - p.kb0);
   p.z = z;
   return p;
-}
-
-// v = act(alpha * acc + beta * c + bias) for 32 consecutive columns of one row.
-__device__ __forceinline__ void store_row32(const float* acc, float* crow, const float* bias, int col0, int N,
-                                            float alpha, float beta, int act, bool raw) {
-  const bool vec = ((reinterpret_cast<uintptr_t>(crow + col0) & 15u) == 0) && (col0 + 32 <= N);
-  if (vec) {
-#pragma unroll
-    for (int j = 0; j < 32; j += 4) {
-      float4 v = make_float4(acc[j], acc[j + 1], acc[j + 2], acc[j + 3]);
-      if (!raw) {
-        float* pv = &v.x;
-        float4 old = beta != 0.f ? *reinterpret_cast<const float4*>(crow + col0 + j) : make_float4(0, 0, 0, 0);
-        const float* po = &old.x;
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          float x = alpha * pv[t];
-          if (beta != 0.f) x += beta * po[t];
-          if (bias) x += bias[col0 + j + t];
-          if (act == VKC_ACT_RELU) x = fmaxf(x, 0.f);
-          else if (act == VKC_ACT_SIGMOID) x = 1.0f / (1.0f + expf(0.0f - x));
-          pv[t] = x;
-        }
-      }
-      *reinterpret_cast<float4*>(crow + col0 + j) = v;
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int col = col0 + j;
-      if (col < N) {
-        float x = acc[j];
-        if (!raw) {
-          x = alpha * x;
-          if (beta != 0.f) x += beta * crow[col];
-          if (bias) x += bias[col];
-          if (act == VKC_ACT_RELU) x = fmaxf(x, 0.f);
-          else if (act == VKC_ACT_SIGMOID) x = 1.0f / (1.0f + expf(0.0f - x));
-        }
-        crow[col] = x;
-      }
-    }
-  }
 }
 
 template <bool X3, int BN, int STAGES, int DRAIN>
@@ -331,21 +290,17 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
       }
       if (!ok) break;
       if (ngroups == 0) continue;
-      const int row = p.m0 + q * 32 + lane;
       const bool raw_out = partial != nullptr;
-      float* crow = raw_out ? partial + ((int64_t)p.z * M + row) * N : C + (int64_t)row * ldc;
+      float* cbase = raw_out ? partial + (int64_t)p.z * M * N : C;
+      const int64_t ld = raw_out ? (int64_t)N : ldc;
+      float* stage = reinterpret_cast<float*>(gbase + Cfg::kEpiOff) + (warp - 2) * (kEpiStageBytes / 4);
 #pragma unroll 1
-      for (int c = 0; c < CW / 32; c += 2) {
-        const uint32_t ta = tmem + lane_addr + (uint32_t)(b * BN + h * CW + c * 32);
-        uint32_t r0[32], r1[32];
-        tmem_ld32_nw(ta, r0);
-        tmem_ld32_nw(ta + 32, r1);
-        tmem_wait_ld();
+      for (int c = 0; c < CW / 32; ++c) {  // one copy of the epilogue code
+        uint32_t r0[32];
+        tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + h * CW + c * 32), r0);
         const int col0 = p.n0 + h * CW + c * 32;
-        if (row < M && col0 < N)
-          store_row32(reinterpret_cast<const float*>(r0), crow, bias, col0, N, alpha, beta, act, raw_out);
-        if (row < M && col0 + 32 < N)
-          store_row32(reinterpret_cast<const float*>(r1), crow, bias, col0 + 32, N, alpha, beta, act, raw_out);
+        if (p.m0 + q * 32 < M && col0 < N)
+          epilogue_tile32(r0, stage, cbase, nullptr, bias, ld, p.m0 + q * 32, M, col0, N, alpha, beta, act, raw_out);
       }
       tc_fence_before();
       __syncwarp();

@@ -22,6 +22,7 @@
 #include "colsum.cuh"
 #include "gemm_simt.cuh"
 #include "tc_ptx.cuh"
+#include "tc_epilogue.cuh"
 
 #include <cuda_bf16.h>
 
@@ -197,7 +198,8 @@ template <bool X3>
 struct GroupedCfg {
   static constexpr uint32_t kStageBytes = (X3 ? 4u : 2u) * kTileBytes;
   static constexpr uint32_t kBarBytes = 8u * (2 * kGroupedStages + 2 * kAccBufs + 1) + 16;
-  static constexpr uint32_t kSmem = kGroupedStages * kStageBytes + 1024 + 256;
+  static constexpr uint32_t kEpiOff = kGroupedStages * kStageBytes + (kBarBytes + 127) / 128 * 128;
+  static constexpr uint32_t kSmem = kEpiOff + 4 * kEpiStageBytes + 1024;
 };
 
 // One CTA per SM walks the tile list.  The stage ring and the TMEM buffer
@@ -379,30 +381,15 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
         }
       }
       if (!ok) break;
-      const int row = m0 + q * 32 + lane;
-      float* crow = P.c + (int64_t)row * P.ldc;
-      const float* mrow = P.mask ? P.mask + (int64_t)row * P.ldc : nullptr;
+      float* stage = reinterpret_cast<float*>(gbase + Cfg::kEpiOff) + (warp - 2) * (kEpiStageBytes / 4);
 #pragma unroll 1
-      for (int c = 0; c < BN / 32; c += 2) {
-        uint32_t r[2][32];
-        tmem_ld32_nw(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r[0]);
-        tmem_ld32_nw(tmem + lane_addr + (uint32_t)(b * BN + c * 32 + 32), r[1]);
-        tmem_wait_ld();
-        if (row < P.m) {
-#pragma unroll
-          for (int j = 0; j < 64; ++j) {
-            const int col = n0 + c * 32 + j;
-            if (col < P.n) {
-              float v = P.alpha * __uint_as_float(r[j >> 5][j & 31]);
-              if (P.beta != 0.f) v += P.beta * crow[col];
-              if (P.bias) v += P.bias[col];
-              if (P.act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
-              else if (P.act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-              if (mrow) v = relu_mask(v, mrow[col]);
-              crow[col] = v;
-            }
-          }
-        }
+      for (int c = 0; c < BN / 32; ++c) {  // one copy of the epilogue code
+        uint32_t r[32];
+        tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r);
+        const int col0 = n0 + c * 32;
+        if (m0 + q * 32 < P.m && col0 < P.n)
+          epilogue_tile32(r, stage, P.c, P.mask, P.bias, P.ldc, m0 + q * 32, P.m, col0, P.n, P.alpha, P.beta, P.act,
+                          false);
       }
       tc_fence_before();
       __syncwarp();

@@ -1,0 +1,75 @@
+// Epilogue of the tensor-core GEMMs: one warp's 32 rows x 32 columns.
+//
+// tcgen05.ld gives each lane one row (32 consecutive columns).  Stored from
+// there, every warp store instruction would touch 32 rows (32 partial
+// sectors); instead the block goes through a 4 KB per-warp shared-memory
+// stage (16-byte chunks XOR-swizzled by row, conflict-free both ways) and
+// comes back with lane = column, so each store writes 128 contiguous bytes of
+// one row and the bias / C / mask reads are coalesced the same way.
+//   v = act(alpha * acc + beta * C + bias), then (grouped backward)
+//   v *= ReLU'(mask); `raw` stores acc unchanged (split-K partials).
+#pragma once
+#include "gemm_simt.cuh"
+
+namespace vkc {
+namespace {
+
+constexpr uint32_t kEpiStageBytes = 32 * 32 * 4;  // per epilogue warp
+
+__device__ __forceinline__ float epi_value(float a, float alpha, float beta, float c, bool has_bias, float b, int act,
+                                           bool has_mask, float m) {
+  float v = alpha * a;
+  if (beta != 0.f) v += beta * c;
+  if (has_bias) v += b;
+  if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+  else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+  if (has_mask) v = relu_mask(v, m);
+  return v;
+}
+
+// acc: this lane's row (row0 + lane), columns col0 .. col0+31.  C / mask
+// point at row 0 of the matrix (leading dimension ld); rows >= M and columns
+// >= N are skipped.  All 32 lanes must call it (warp-synchronous).
+__device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float* __restrict__ stage, float* C,
+                                                const float* mask, const float* __restrict__ bias, int64_t ld,
+                                                int row0, int M, int col0, int N, float alpha, float beta, int act,
+                                                bool raw) {
+  const int lane = threadIdx.x & 31;
+  float4* srow = reinterpret_cast<float4*>(stage) + lane * 8;
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    srow[q ^ (lane & 7)] = make_float4(__uint_as_float(acc[4 * q]), __uint_as_float(acc[4 * q + 1]),
+                                       __uint_as_float(acc[4 * q + 2]), __uint_as_float(acc[4 * q + 3]));
+  __syncwarp();
+  const int col = col0 + lane;
+  const bool cin = col < N;
+  const int rows = min(32, M - row0);
+  const bool hb = bias != nullptr, hm = mask != nullptr, hc = beta != 0.f && !raw;
+  const float b = (hb && cin) ? bias[col] : 0.f;
+  auto staged = [&](int j) { return stage[j * 32 + ((((lane >> 2) ^ j) & 7) << 2) + (lane & 3)]; };
+#pragma unroll 1
+  for (int j0 = 0; j0 < rows; j0 += 16) {
+    // the group's loads before its stores (a load after a store to C could
+    // not be hoisted: the pointers may alias); 16 rows per group, so a
+    // 32-row block waits for memory twice
+    float cv[16], mv[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int64_t off = (int64_t)(row0 + j0 + t) * ld + col;
+      const bool in = cin && j0 + t < rows;
+      cv[t] = (in && hc) ? C[off] : 0.f;
+      mv[t] = (in && hm) ? mask[off] : 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      if (cin && j0 + t < rows) {
+        const float a = staged(j0 + t);
+        C[(int64_t)(row0 + j0 + t) * ld + col] = raw ? a : epi_value(a, alpha, beta, cv[t], hb, b, act, hm, mv[t]);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+}  // namespace
+}  // namespace vkc
