@@ -441,7 +441,7 @@ def mlp_study(vk, gpu, timer, steps=50, precisions=("fp32", "bf16x3")):
     return res
 
 
-def batched_study(vk, gpu, timer, n_models=64, steps=10):
+def batched_study(vk, gpu, timer, n_models=64, steps=10, precisions=("fp32", "bf16x3")):
     """64 independent 2-layer MLPs of uneven sizes (seed 2: input width in
     [17,1021], hidden in [32,2048], output in [2,64], batch in [1,512]),
     Dense-ReLU-Dense, MSE loss, SGD(1e-2).  One step trains all 64 models.
@@ -487,7 +487,7 @@ def batched_study(vk, gpu, timer, n_models=64, steps=10):
         return {"steps_per_s": round(1000.0 / ms, 1), "ms_per_step": round(ms, 3),
                 "tflops": round(flop / (ms * 1e-3) / 1e12, 2)}
 
-    for prec in ("fp32", "bf16x3"):
+    for prec in precisions:
         gpu.matmul_precision = prec
         nets = build(7)
         def eager():
@@ -518,10 +518,11 @@ def batched_study(vk, gpu, timer, n_models=64, steps=10):
         res[f"grouped_graph_{prec}"] = timed(g.launch, steps * 5)
         del g, grp, nets
     gpu.matmul_precision = "fp32"
-    res["speedup_graph_bf16x3_vs_eager_fp32"] = round(res["graph_bf16x3"]["steps_per_s"] /
-                                                      res["eager_fp32"]["steps_per_s"], 2)
-    res["speedup_grouped_graph_bf16x3_vs_eager_fp32"] = round(res["grouped_graph_bf16x3"]["steps_per_s"] /
-                                                              res["eager_fp32"]["steps_per_s"], 2)
+    if "eager_fp32" in res and "graph_bf16x3" in res:
+        res["speedup_graph_bf16x3_vs_eager_fp32"] = round(res["graph_bf16x3"]["steps_per_s"] /
+                                                          res["eager_fp32"]["steps_per_s"], 2)
+        res["speedup_grouped_graph_bf16x3_vs_eager_fp32"] = round(res["grouped_graph_bf16x3"]["steps_per_s"] /
+                                                                  res["eager_fp32"]["steps_per_s"], 2)
     return res
 
 
@@ -931,6 +932,8 @@ def run_study(args):
                             precisions=tuple(args.mm_precisions.split(",")))
     if args.study == "mlp":
         return mlp_study(vk, gpu, timer, precisions=tuple(args.mm_precisions.split(",")))
+    if args.study == "batched":
+        return batched_study(vk, gpu, timer, precisions=tuple(args.mm_precisions.split(",")))
     fn = {"batched": batched_study, "chain": chain_study,
           "reduction_precision": reduction_precision_study, "small_suite": small_suite_study}.get(args.study)
     if fn is None:

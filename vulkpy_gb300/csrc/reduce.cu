@@ -348,9 +348,19 @@ __global__ void k_combine_splits(const double* partials, size_t prev, size_t axi
   size_t i = idx / post, j = idx % post;
   Acc<OP, COMP> acc;
   acc.init();
-  for (int s = 0; s < splits; ++s) {
-    size_t p = (i * splits + s) * post + j;
-    acc.merge((float)partials[2 * p], (float)partials[2 * p + 1]);
+  // eight splits' partials loaded ahead of their (ordered) merges: one
+  // memory wait per eight instead of one per split
+  for (int s0 = 0; s0 < splits; s0 += 8) {
+    double pv[8], pc[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const size_t p = (i * splits + s0 + t) * post + j;
+      pv[t] = s0 + t < splits ? partials[2 * p] : 0.0;
+      pc[t] = s0 + t < splits ? partials[2 * p + 1] : 0.0;
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if (s0 + t < splits) acc.merge((float)pv[t], (float)pc[t]);
   }
   float v = acc.value();
   if (OP == VKC_SUM || OP == VKC_PROD) v *= scale;
