@@ -257,9 +257,10 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
         b = acc_it & 1;
         if (*abort_flag || !mbar_wait(accf_bar(b), (acc_it >> 1) & 1)) { ok = false; break; }
         tc_fence_after();
-        if (X3) {
+        if (X3 && ngroups > 1) {
           // add this accumulation to the fp32 sums; after the last one, put
-          // the sums back into the buffer for the store loop below
+          // the sums back into the buffer for the store loop below (with a
+          // single accumulation the store loop reads it as it is)
           const bool last = gi == ngroups - 1;
 #pragma unroll
           for (int c = 0; c < CW / 32; c += 2) {

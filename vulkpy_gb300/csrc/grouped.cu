@@ -193,20 +193,25 @@ struct TcTable {
 };
 
 constexpr int kGroupedStages = 3;
+// warps: 0 producer, 1 TMEM owner + MMA issuer, 2..9 epilogue (two per TMEM
+// lane quarter, 64 columns each: the per-tile epilogue is the critical path
+// of the short-K tiles, so it gets eight warps)
+constexpr int kGroupedEpiWarps = 8;
+constexpr int kThreadsGrouped = 32 * (2 + kGroupedEpiWarps);
 
 template <bool X3>
 struct GroupedCfg {
   static constexpr uint32_t kStageBytes = (X3 ? 4u : 2u) * kTileBytes;
   static constexpr uint32_t kBarBytes = 8u * (2 * kGroupedStages + 2 * kAccBufs + 1) + 16;
   static constexpr uint32_t kEpiOff = kGroupedStages * kStageBytes + (kBarBytes + 127) / 128 * 128;
-  static constexpr uint32_t kSmem = kEpiOff + 4 * kEpiStageBytes + 1024;
+  static constexpr uint32_t kSmem = kEpiOff + kGroupedEpiWarps * kEpiStageBytes + 1024;
 };
 
 // One CTA per SM walks the tile list.  The stage ring and the TMEM buffer
 // ring continue across tiles (a running K-block counter gives every slot and
 // parity), so the next tile's copies and MMAs overlap this tile's epilogue.
 template <bool X3>
-__global__ void __launch_bounds__(kThreadsTC, 1)
+__global__ void __launch_bounds__(kThreadsGrouped, 1)
 k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
   constexpr int BN = 128;
   constexpr int S = kGroupedStages;
@@ -234,7 +239,7 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
     }
     for (int b = 0; b < kAccBufs; ++b) {
       mbar_init(accf_bar(b), 1);
-      mbar_init(acce_bar(b), 4);
+      mbar_init(acce_bar(b), kGroupedEpiWarps);
     }
     mbar_init(drain_bar, 1);
     *abort_flag = 0;
@@ -331,30 +336,32 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
     // loop reads them 32 columns at a time (not unrolled), so the epilogue
     // code exists once instead of 128 times (instruction fetch dominated
     // small launches with the unrolled form).
-    const int q = warp & 3;
-    const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
+    constexpr int CW = BN / 2;        // columns per epilogue warp
+    const int q = warp & 3;           // TMEM lane quarter
+    const int hc = (warp - 2) >> 2;   // column half
+    const uint32_t lane_addr = ((uint32_t)(q * 32) << 16) + (uint32_t)(hc * CW);
     uint32_t g = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
       const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
       const int local = t - P.tile0;
-      const int m0 = (local / P.tiles_n) * kTileRows, n0 = (local % P.tiles_n) * BN;
+      const int m0 = (local / P.tiles_n) * kTileRows, n0 = (local % P.tiles_n) * BN + hc * CW;
       const int span = X3 ? kDrainX3 : P.kt;
       const int ngroups = (P.kt + span - 1) / span;
-      float sum[X3 ? BN : 1];
+      float sum[X3 ? CW : 1];
       if (X3) {
 #pragma unroll
-        for (int j = 0; j < (X3 ? BN : 1); ++j) sum[j] = 0.f;
+        for (int j = 0; j < (X3 ? CW : 1); ++j) sum[j] = 0.f;
       }
       int b = 0;
       for (int gi = 0; gi < ngroups; ++gi, ++g) {
         b = g % kAccBufs;
         if (*abort_flag || !mbar_wait(accf_bar(b), (g / kAccBufs) & 1)) { ok = false; break; }
         tc_fence_after();
-        if (X3) {
+        if (X3 && ngroups > 1) {  // one accumulation: the store loop reads it from TMEM as it is
           const bool last = gi == ngroups - 1;
 #pragma unroll
-          for (int c = 0; c < BN / 32; c += 2) {
+          for (int c = 0; c < CW / 32; c += 2) {
             const uint32_t ta = tmem + lane_addr + (uint32_t)(b * BN + c * 32);
             uint32_t r0[32], r1[32];
             tmem_ld32_nw(ta, r0);
@@ -383,7 +390,7 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
       if (!ok) break;
       float* stage = reinterpret_cast<float*>(gbase + Cfg::kEpiOff) + (warp - 2) * (kEpiStageBytes / 4);
 #pragma unroll 1
-      for (int c = 0; c < BN / 32; ++c) {  // one copy of the epilogue code
+      for (int c = 0; c < CW / 32; ++c) {  // one copy of the epilogue code
         uint32_t r[32];
         tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r);
         const int col0 = n0 + c * 32;
@@ -750,7 +757,7 @@ int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const s
                                GroupedCfg<true>::kSmem);
           attr = true;
         }
-        k_gemm_tc_grouped<true><<<grid, kThreadsTC, GroupedCfg<true>::kSmem, dev->stream>>>(tab, dev->err_word);
+        k_gemm_tc_grouped<true><<<grid, kThreadsGrouped, GroupedCfg<true>::kSmem, dev->stream>>>(tab, dev->err_word);
       } else {
         static bool attr = false;
         if (!attr) {
@@ -758,7 +765,7 @@ int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const s
                                GroupedCfg<false>::kSmem);
           attr = true;
         }
-        k_gemm_tc_grouped<false><<<grid, kThreadsTC, GroupedCfg<false>::kSmem, dev->stream>>>(tab, dev->err_word);
+        k_gemm_tc_grouped<false><<<grid, kThreadsGrouped, GroupedCfg<false>::kSmem, dev->stream>>>(tab, dev->err_word);
       }
       r = check_launch("gemm_grouped (tensor cores)");
     }
