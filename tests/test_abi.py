@@ -64,3 +64,19 @@ def test_gemm_tuning_table_host_side(tmp_path):
     assert _lib.lib.vkc_gemm_tune_clear() == _lib.OK
     autotune.load_table()   # restore the shipped table
     assert autotune.bucket(1) == 0 and autotune.bucket(784) == 10 and autotune.bucket(1024) == 10
+
+
+def test_grouped_entry_points_validate_without_gpu():
+    """The one-launch-per-step entry points reject a missing device and bad
+    arguments before touching the GPU."""
+    import ctypes as C
+    from vulkpy_gb300 import _lib
+    L = _lib.lib
+    ptrs = (C.c_void_p * 1)(None)
+    n = (C.c_int64 * 1)(4)
+    assert L.vkc_fill_f32_grouped(None, ptrs, n, 0.0, 1) == _lib.ERR_INVALID
+    assert L.vkc_adam_update_grouped(None, ptrs, ptrs, ptrs, ptrs, ptrs, n, 1, 1e-3, 0.9, 0.999, 1e-8) \
+        == _lib.ERR_INVALID
+    assert L.vkc_sgd_update_grouped(None, ptrs, ptrs, n, 1e-2, 1) == _lib.ERR_INVALID
+    s, t = C.c_int(), C.c_int()
+    assert L.vkc_gemm_plan_get(None, _lib.MM_BF16X3, 256, 1024, 784, C.byref(s), C.byref(t)) == _lib.ERR_INVALID
