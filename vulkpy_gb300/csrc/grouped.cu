@@ -482,13 +482,36 @@ __device__ __forceinline__ int find_vec(const VecTable& tab, int t) {
   return lo;
 }
 
-// value += (-lr) * grad, as the single-tensor SGD kernel computes it.
+// value += (-lr) * grad, as the single-tensor SGD kernel computes it; 16-byte
+// accesses when both tensors are 16-byte aligned.
 __global__ void __launch_bounds__(256) k_sgd_grouped(const __grid_constant__ VecTable tab) {
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
     const VecItem& I = tab.it[find_vec(tab, t)];
     const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
     const int64_t i1 = min(i0 + kVecChunk, I.n);
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) I.value[i] = __fadd_rn(I.value[i], __fmul_rn(I.scale, I.grad[i]));
+    const bool vec = ((reinterpret_cast<uintptr_t>(I.value) | reinterpret_cast<uintptr_t>(I.grad)) & 15u) == 0;
+    if (vec && i1 - i0 == kVecChunk) {  // kVecChunk = 4096 = 256 threads x 4 float4
+      float4 vv[4], gg[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + (int64_t)(u * 256 + threadIdx.x) * 4;
+        vv[u] = *reinterpret_cast<const float4*>(I.value + i);
+        gg[u] = *reinterpret_cast<const float4*>(I.grad + i);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + (int64_t)(u * 256 + threadIdx.x) * 4;
+        float4 o;
+        o.x = __fadd_rn(vv[u].x, __fmul_rn(I.scale, gg[u].x));
+        o.y = __fadd_rn(vv[u].y, __fmul_rn(I.scale, gg[u].y));
+        o.z = __fadd_rn(vv[u].z, __fmul_rn(I.scale, gg[u].z));
+        o.w = __fadd_rn(vv[u].w, __fmul_rn(I.scale, gg[u].w));
+        *reinterpret_cast<float4*>(I.value + i) = o;
+      }
+    } else {
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += 256)
+        I.value[i] = __fadd_rn(I.value[i], __fmul_rn(I.scale, I.grad[i]));
+    }
   }
 }
 
