@@ -374,6 +374,27 @@ def matmul_study(vk, gpu, timer, sizes=(4096, 8192), precisions=("fp32", "bf16",
             out[f"{prec}_{n}"] = {"tflops": round(2 * n ** 3 / (ms * 1e-3) / 1e12, 1), "ms": round(ms, 3),
                                   "rel_err_fp64": float(f"{err:.3g}")}
         del a, b, c
+    # 1-D @ 2-D: (8192,) @ (8192, 8192), an HBM-bound matrix-vector product
+    # (fp32 GEMV for every precision); GB/s counts the matrix once
+    n = sizes[-1]
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal(n, dtype=np.float32)
+    B = rng.standard_normal((n, n), dtype=np.float32)
+    ref = v.astype(np.float64) @ B.astype(np.float64)
+    a, b = vk.Array(gpu, data=v), vk.Array(gpu, data=B)
+    c = a @ b
+    gpu.wait()
+    t0 = timer.mark()
+    for _ in range(10):
+        c = a @ b
+    t1 = timer.mark()
+    gpu.wait()
+    ms = timer.ms(t0, t1) / 10
+    timer.free(t0, t1)
+    err = float(np.linalg.norm(np.asarray(c) - ref) / np.linalg.norm(ref))
+    out[f"gemv_1d_{n}"] = {"gbs": round(4 * n * n / (ms * 1e-3) / 1e9, 1), "ms": round(ms, 4),
+                           "tflops": round(2 * n * n / (ms * 1e-3) / 1e12, 2), "rel_err_fp64": float(f"{err:.3g}")}
+    del a, b, c
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak = json.load(open(peaks_path))["bf16_tflops"] if os.path.exists(peaks_path) else 1900.0
     best = out.get(f"bf16x3_{sizes[-1]}", {}).get("tflops")

@@ -145,6 +145,28 @@ k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restric
                     (int64_t)blockIdx.x * kGemmBN, sm);
 }
 
+// Matrix-vector product (gemv.cu): y[j] = act(alpha * sum_k Mat(j, k) vec[k]
+// + beta * y[j] + bias[j * bias_stride]); Mat(j, k) = P[j*ld + k] when
+// `kcontig`, else P[k*ld + j]; vec[k] at vec[k * vs]; y[j] at y[j * ys].
+int gemv(vkc_device_t dev, bool kcontig, int64_t J, int64_t K, float alpha, const float* P, int64_t ld,
+         const float* vec, int64_t vs, float beta, float* y, int64_t ys, const float* bias, int64_t bias_stride,
+         int act);
+
+// A GEMM with M == 1 or N == 1 as a matrix-vector product; returns -1 when
+// the operands do not fit gemv (the caller then runs the tiled GEMM).
+inline int gemm_as_gemv(vkc_device_t dev, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
+                        const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                        const GemmEpilogue& epi) {
+  if (K == 0 || (M != 1 && N != 1)) return -1;
+  if (M == 1) {
+    // y[n] = sum_k op(A)(0, k) op(B)(k, n); op(B)(k, n) = tb ? B[n*ldb + k] : B[k*ldb + n]
+    return gemv(dev, tb, N, K, alpha, B, ldb, A, ta ? lda : 1, beta, C, 1, epi.bias, 1, epi.act);
+  }
+  // N == 1: y[m] = sum_k op(A)(m, k) op(B)(k, 0); op(A)(m, k) = ta ? A[k*lda + m] : A[m*lda + k]
+  if (ta && ldc != 1) return -1;
+  return gemv(dev, !ta, M, K, alpha, A, lda, B, tb ? 1 : ldb, beta, C, ldc, epi.bias, 0, epi.act);
+}
+
 inline int gemm_simt(vkc_device_t dev, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
                      const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
                      GemmEpilogue epi) {

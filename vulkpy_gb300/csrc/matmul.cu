@@ -13,6 +13,12 @@ VKC_EXPORT int vkc_gemm(vkc_device_t dev, int precision, int trans_a, int trans_
   VKC_REQUIRE(c && (k == 0 || (a && b)), "NULL buffer");
   VKC_REQUIRE(ldc >= n, "ldc < n");
   VKC_REQUIRE(lda >= (trans_a ? m : k) && ldb >= (trans_b ? k : n), "leading dimension too small");
+  // vectors (M == 1 or N == 1) in fp32 for every precision: bound by reading the matrix
+  if (precision == VKC_MM_FP32 || precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3) {
+    const int r = vkc::gemm_as_gemv(dev, trans_a != 0, trans_b != 0, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,
+                                    vkc::GemmEpilogue{});
+    if (r >= 0) return r;
+  }
   switch (precision) {
     case VKC_MM_FP32:
       return vkc::gemm_simt(dev, trans_a != 0, trans_b != 0, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc,

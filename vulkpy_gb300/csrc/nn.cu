@@ -23,6 +23,10 @@ constexpr int kThreads = 256;
 int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
              const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
              vkc::GemmEpilogue epi) {
+  if (precision == VKC_MM_FP32 || precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3) {
+    const int r = vkc::gemm_as_gemv(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+    if (r >= 0) return r;
+  }
   if (precision == VKC_MM_FP32)
     return vkc::gemm_simt(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
   if (precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3)
