@@ -137,6 +137,73 @@ k_gemv_jcontig(int64_t J, int64_t K, float alpha, const float* __restrict__ P, i
   }
 }
 
+// Aligned J-contiguous case (ld % 4 == 0, J % 4 == 0, 16-byte aligned P):
+// a block owns 128 columns (lane = four columns) and rows [k0, k1) of split
+// blockIdx.y, divided among its 8 warps in 8 contiguous slices; the warps'
+// sums are added in warp order through shared memory.  Few splits, so the
+// combine pass adds few partials.
+__global__ void __launch_bounds__(256)
+k_gemv_jcontig8(int64_t J, int64_t K, float alpha, const float* __restrict__ P, int64_t ld,
+                const float* __restrict__ vec, int64_t vs, float beta, float* y, const float* __restrict__ bias,
+                int64_t bias_stride, int act, float* __restrict__ partial, int64_t span) {
+  __shared__ float4 part[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t j = ((int64_t)blockIdx.x * 32 + lane) * 4;
+  const int64_t k0 = (int64_t)blockIdx.y * span, k1 = min(K, k0 + span);
+  const int64_t sub = (k1 - k0 + 7) / 8;
+  const int64_t a0 = k0 + w * sub, a1 = min(k1, a0 + sub);
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (j < J) {
+    int64_t k = a0;
+    for (; k + 7 < a1; k += 8) {  // eight rows' loads in flight
+      float4 m[8];
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        m[u] = __ldcs(reinterpret_cast<const float4*>(P + (k + u) * ld + j));
+        v[u] = vec[(k + u) * vs];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        s.x = fmaf(m[u].x, v[u], s.x);
+        s.y = fmaf(m[u].y, v[u], s.y);
+        s.z = fmaf(m[u].z, v[u], s.z);
+        s.w = fmaf(m[u].w, v[u], s.w);
+      }
+    }
+    for (; k < a1; ++k) {
+      const float4 m = __ldcs(reinterpret_cast<const float4*>(P + k * ld + j));
+      const float v = vec[k * vs];
+      s.x = fmaf(m.x, v, s.x);
+      s.y = fmaf(m.y, v, s.y);
+      s.z = fmaf(m.z, v, s.z);
+      s.w = fmaf(m.w, v, s.w);
+    }
+  }
+  part[w][lane] = s;
+  __syncthreads();
+  if (w != 0 || j >= J) return;
+  float4 t = part[0][lane];
+#pragma unroll
+  for (int q = 1; q < 8; ++q) {
+    const float4 p = part[q][lane];
+    t.x += p.x;
+    t.y += p.y;
+    t.z += p.z;
+    t.w += p.w;
+  }
+  if (partial) {
+    *reinterpret_cast<float4*>(partial + (int64_t)blockIdx.y * J + j) = t;
+  } else {
+    const float r[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float* out = y + j + q;
+      *out = gemv_epilogue(r[q], alpha, beta, out, bias != nullptr, bias ? bias[(j + q) * bias_stride] : 0.f, act);
+    }
+  }
+}
+
 // y[j] = epilogue(sum over splits in order of partial[s][j]).
 __global__ void __launch_bounds__(256)
 k_gemv_combine(const float* __restrict__ partial, int splits, int64_t J, float alpha, float beta, float* y,
@@ -176,6 +243,29 @@ int gemv(vkc_device_t dev, bool kcontig, int64_t J, int64_t K, float alpha, cons
     return check_launch("gemv");
   }
   VKC_REQUIRE(ys == 1, "gemv: strided output with a J-contiguous matrix");
+  if (J % 4 == 0 && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(P) & 15u) == 0) {
+    const int64_t blocks_x = (J + 127) / 128;
+    const int64_t per_sm = resident_blocks((const void*)k_gemv_jcontig8, 256);
+    int64_t splits = std::max<int64_t>(1, std::min<int64_t>((int64_t)dev->sm_count * per_sm / blocks_x, K / 64));
+    splits = std::min<int64_t>(splits, 65535);
+    const int64_t span = (K + splits - 1) / splits;
+    splits = std::max<int64_t>(1, (K + span - 1) / span);
+    float* partial = nullptr;
+    if (splits > 1) {
+      int r = scratch_alloc(dev, sizeof(float) * (size_t)splits * J, (void**)&partial);
+      if (r != VKC_OK) return r;
+    }
+    k_gemv_jcontig8<<<dim3((unsigned)blocks_x, (unsigned)splits), 256, 0, dev->stream>>>(
+        J, K, alpha, P, ld, vec, vs, beta, y, bias, bias_stride, act, partial, span);
+    int r = check_launch("gemv");
+    if (r == VKC_OK && partial) {
+      k_gemv_combine<<<(unsigned)((J + 255) / 256), 256, 0, dev->stream>>>(partial, (int)splits, J, alpha, beta, y,
+                                                                           bias, bias_stride, act);
+      r = check_launch("gemv combine");
+    }
+    scratch_free(dev, partial);
+    return r;
+  }
   const int64_t threads = (J + 3) / 4;
   const int64_t blocks_x = (threads + 255) / 256;
   // about four 256-thread blocks per SM: each thread keeps 128 bytes of
