@@ -305,3 +305,22 @@ def test_matmul_vector_forms(gpu, vk):
     np.testing.assert_allclose(np.asarray(vk.Array(gpu, data=w) @ vk.Array(gpu, data=A)), w @ A, rtol=1e-5, atol=1e-5)
     with pytest.raises(ValueError):
         vk.Array(gpu, data=A) @ vk.Array(gpu, data=A)
+
+
+@pytest.mark.parametrize("size,n", [(1, 20000), (2, 300000), (64, 65536), (64, 65537), (6, 1 << 20), (1000, 777777),
+                                    (64, 1 << 20)])
+def test_prng_segmented_streams(gpu, vk, size, n):
+    """Few states, long streams: generation is split into segments whose
+    start states come from powers of the next() map; the outputs and the
+    final states are those of the serial chain (bit-exact with the oracle),
+    and a second call continues the stream."""
+    r = vk.random.Xoshiro128pp(gpu, size=size, seed=11)
+    ref = O.Xoshiro128pp(11, size)
+    np.testing.assert_array_equal(np.asarray(r.randint(shape=(n,))), ref.u32(n))
+    np.testing.assert_array_equal(r.state().reshape(-1), ref.state)
+    np.testing.assert_array_equal(np.asarray(r.random(shape=(n // 3,))), ref.f32(n // 3))
+    np.testing.assert_array_equal(r.state().reshape(-1), ref.state)
+    if size % 2 == 0:
+        got = np.asarray(r.normal(shape=(n // 2,), mean=0.5, stddev=3.0))
+        np.testing.assert_allclose(got, ref.normal(n // 2, 0.5, 3.0), rtol=2e-6, atol=6e-6)
+        np.testing.assert_array_equal(r.state().reshape(-1), ref.state)

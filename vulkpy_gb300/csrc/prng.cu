@@ -123,6 +123,25 @@ int ensure_jump_powers(vkc_device_t dev) {
   return VKC_OK;
 }
 
+// Powers of the next() map itself, N^(2^k): with few states a state's chain
+// of outputs is cut into segments whose start states are N^(g L) s, so the
+// segments run in parallel (outputs and final states are those of the
+// serial loop).
+constexpr int kNextPowers = 48;  // up to 2^48 steps per state
+int ensure_next_powers(vkc_device_t dev) {
+  if (dev->xo_next_pows) return VKC_OK;
+  static std::vector<uint32_t> host_pows = powers(matrix_of([](uint32_t* s) { host_step(s); }), kNextPowers);
+  uint32_t* d = nullptr;
+  VKC_CUDA(cudaMalloc(&d, host_pows.size() * sizeof(uint32_t)));
+  cudaError_t e = cudaMemcpy(d, host_pows.data(), host_pows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return vkc::set_error(VKC_ERR_CUDA, "next powers upload: %s", cudaGetErrorString(e));
+  }
+  dev->xo_next_pows = d;
+  return VKC_OK;
+}
+
 // ---------------------------------------------------------------- device side
 __device__ __forceinline__ uint32_t rotl(uint32_t x, int k) { return __funnelshift_l(x, x, k); }
 
@@ -186,7 +205,51 @@ k_seed(uint4 s0, const uint4* __restrict__ jump_pows, uint32_t size, uint4* stat
   state[i] = x;
 }
 
+// s advanced by e steps of next(): N^e s from the powers N^(2^k).
+__device__ __forceinline__ uint4 advance(const uint4* __restrict__ pows, uint4 s, uint64_t e) {
+  int k = 0;
+  while (e) {
+    if (e & 1u) s = apply_dev(pows + (size_t)k * 128, s);
+    e >>= 1;
+    ++k;
+  }
+  return s;
+}
+
 enum { kOutU32 = 0, kOutF32 = 1, kOutRange = 2 };
+
+template <int MODE>
+__device__ __forceinline__ void put(void* out, size_t k, uint32_t r, uint32_t low, uint32_t range) {
+  if (MODE == kOutU32) {
+    static_cast<uint32_t*>(out)[k] = r;
+  } else if (MODE == kOutF32) {
+    static_cast<float*>(out)[k] = to_unit(r);
+  } else {
+    // prng_randrange.comp:26: low + uint(float(range) * u)
+    static_cast<uint32_t*>(out)[k] = low + (uint32_t)((float)range * to_unit(r));
+  }
+}
+
+// Segmented generation: thread (t, g) = (idx % size, idx / size) produces
+// steps [g L, (g + 1) L) of state t (out[step * size + t]); the thread
+// holding a state's last step stores it to state_out (state_in is read by
+// every segment, so it is not overwritten here).
+template <int MODE>
+__global__ void __launch_bounds__(kThreads)
+k_generate_seg(const uint4* __restrict__ state_in, uint4* __restrict__ state_out, uint32_t size, void* out, size_t n,
+               uint32_t low, uint32_t range, const uint4* __restrict__ pows, uint64_t L, uint32_t G) {
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (uint64_t)size * G) return;
+  const uint32_t t = (uint32_t)(idx % size), g = (uint32_t)(idx / size);
+  if ((size_t)t >= n) return;
+  const uint64_t cnt = (n - t + size - 1) / size;  // steps of state t
+  const uint64_t b0 = (uint64_t)g * L;
+  if (b0 >= cnt) return;
+  const uint64_t b1 = min(cnt, b0 + L);
+  uint4 s = advance(pows, state_in[t], b0);
+  for (uint64_t step = b0; step < b1; ++step) put<MODE>(out, step * size + t, next(s), low, range);
+  if (b1 == cnt) state_out[t] = s;
+}
 
 template <int MODE>
 __global__ void __launch_bounds__(kThreads)
@@ -194,17 +257,7 @@ k_generate(uint4* state, uint32_t size, void* out, size_t n, uint32_t low, uint3
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= size || (size_t)t >= n) return;
   uint4 s = state[t];
-  for (size_t k = t; k < n; k += size) {
-    const uint32_t r = next(s);
-    if (MODE == kOutU32) {
-      static_cast<uint32_t*>(out)[k] = r;
-    } else if (MODE == kOutF32) {
-      static_cast<float*>(out)[k] = to_unit(r);
-    } else {
-      // prng_randrange.comp:26: low + uint(float(range) * u)
-      static_cast<uint32_t*>(out)[k] = low + (uint32_t)((float)range * to_unit(r));
-    }
-  }
+  for (size_t k = t; k < n; k += size) put<MODE>(out, k, next(s), low, range);
   state[t] = s;
 }
 
@@ -229,6 +282,37 @@ k_normal_pairs(uint4* state, uint32_t size, float* out, size_t n, size_t m, floa
   state[ta + 1] = sb;
 }
 
+// k_normal_pairs cut into segments of L pair-steps (as k_generate_seg).
+__global__ void __launch_bounds__(kThreads)
+k_normal_pairs_seg(const uint4* __restrict__ state_in, uint4* __restrict__ state_out, uint32_t size, float* out,
+                   size_t n, size_t m, float mean, float stddev, const uint4* __restrict__ pows, uint64_t L,
+                   uint32_t G) {
+  const uint32_t pairs = size / 2;
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (uint64_t)pairs * G) return;
+  const uint32_t p = (uint32_t)(idx % pairs), g = (uint32_t)(idx / pairs);
+  const uint32_t ta = 2 * p;
+  if ((size_t)ta >= m) return;
+  const uint64_t cnt = (m - ta + size - 1) / size;  // pair steps of states ta, ta + 1
+  const uint64_t b0 = (uint64_t)g * L;
+  if (b0 >= cnt) return;
+  const uint64_t b1 = min(cnt, b0 + L);
+  uint4 sa = advance(pows, state_in[ta], b0), sb = advance(pows, state_in[ta + 1], b0);
+  for (uint64_t step = b0; step < b1; ++step) {
+    const size_t k0 = step * size + ta;
+    const float u0 = to_unit(next(sa));
+    const float u1 = to_unit(next(sb));
+    float z0, z1;
+    box_muller(u0, u1, mean, stddev, z0, z1);
+    out[k0] = z0;
+    if (k0 + 1 < n) out[k0 + 1] = z1;
+  }
+  if (b1 == cnt) {
+    state_out[ta] = sa;
+    state_out[ta + 1] = sb;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads)
 k_box_muller(const float* u, float* out, size_t n, float mean, float stddev) {
   const size_t pairs = (n + 1) / 2;
@@ -242,6 +326,51 @@ k_box_muller(const float* u, float* out, size_t n, float mean, float stddev) {
   }
 }
 
+// Segments per state for `active` states of `steps` outputs each: enough
+// threads to fill the GPU, at least `min_len` steps per segment (a segment's
+// start costs one application of a power of N per set bit of its offset, so
+// cheap steps (uniform draws) need longer segments than Box-Muller pairs).
+// 1 = serial chains.
+uint32_t segments(vkc_device_t dev, uint64_t active, uint64_t steps, uint64_t min_len) {
+  const uint64_t want_threads = (uint64_t)dev->sm_count * 512;
+  if (active >= want_threads || steps < 2 * min_len) return 1;
+  if (!dev->xo_next_pows) {
+    // the powers are uploaded synchronously on first use: not while the
+    // stream is being captured (the serial kernel computes the same values)
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(dev->stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
+      cudaGetLastError();
+      return 1;
+    }
+  }
+  const uint64_t g = std::min<uint64_t>((want_threads + active - 1) / active, steps / min_len);
+  return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, 1u << 20));
+}
+
+// Run a segmented kernel: the final states go to a scratch copy (every
+// segment reads the initial ones) and are copied back for the first
+// `active` states (the others do not advance).
+template <class Launch>
+int run_segmented(vkc_device_t dev, uint32_t* state, uint32_t active, Launch launch) {
+  {
+    std::lock_guard<std::mutex> lk(dev->mu);
+    int r = ensure_next_powers(dev);
+    if (r != VKC_OK) return r;
+  }
+  uint4* state_out = nullptr;
+  int r = vkc::scratch_alloc(dev, (size_t)active * sizeof(uint4), (void**)&state_out);
+  if (r != VKC_OK) return r;
+  launch(state_out, reinterpret_cast<const uint4*>(dev->xo_next_pows));
+  r = vkc::check_launch("xoshiro (segmented)");
+  if (r == VKC_OK) {
+    cudaError_t e = cudaMemcpyAsync(state, state_out, (size_t)active * sizeof(uint4), cudaMemcpyDeviceToDevice,
+                                    dev->stream);
+    if (e != cudaSuccess) r = vkc::set_error(VKC_ERR_CUDA, "xoshiro state copy: %s", cudaGetErrorString(e));
+  }
+  vkc::scratch_free(dev, state_out);
+  return r;
+}
+
 template <int MODE>
 int generate(vkc_device_t dev, uint32_t* state, uint32_t size, void* out, size_t n, uint32_t low, uint32_t range) {
   if (n == 0) return VKC_OK;
@@ -249,6 +378,16 @@ int generate(vkc_device_t dev, uint32_t* state, uint32_t size, void* out, size_t
   VKC_REQUIRE(size > 0, "PRNG has no states");
   VKC_REQUIRE(((uintptr_t)state & 15u) == 0, "state buffer must be 16-byte aligned");
   uint32_t active = (uint32_t)std::min<size_t>(size, n);
+  const uint64_t steps = (n + size - 1) / size;
+  const uint32_t G = segments(dev, active, steps, 1024);
+  if (G > 1) {
+    const uint64_t L = (steps + G - 1) / G;
+    return run_segmented(dev, state, active, [&](uint4* state_out, const uint4* pows) {
+      const uint64_t threads = (uint64_t)size * G;
+      k_generate_seg<MODE><<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, dev->stream>>>(
+          reinterpret_cast<const uint4*>(state), state_out, size, out, n, low, range, pows, L, G);
+    });
+  }
   unsigned grid = (active + kThreads - 1) / kThreads;
   k_generate<MODE><<<grid, kThreads, 0, dev->stream>>>(reinterpret_cast<uint4*>(state), size, out, n, low, range);
   return vkc::check_launch("xoshiro");
@@ -314,6 +453,16 @@ VKC_EXPORT int vkc_xoshiro_normal(vkc_device_t dev, uint32_t* state, uint32_t si
   const size_t m = (n % 2 == 0) ? n : n + 1;  // random.py:116-118 draws 2*(n//2+1) for odd n
   if (size % 2 == 0) {
     uint32_t pairs = (uint32_t)std::min<size_t>(size / 2, m / 2);
+    const uint64_t steps = (m + size - 1) / size;
+    const uint32_t G = segments(dev, pairs, steps, 64);
+    if (G > 1) {
+      const uint64_t L = (steps + G - 1) / G;
+      return run_segmented(dev, state, (uint32_t)std::min<size_t>(size, m), [&](uint4* state_out, const uint4* pows) {
+        const uint64_t threads = (uint64_t)(size / 2) * G;
+        k_normal_pairs_seg<<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, dev->stream>>>(
+            reinterpret_cast<const uint4*>(state), state_out, size, out, n, m, mean, stddev, pows, L, G);
+      });
+    }
     unsigned grid = (pairs + kThreads - 1) / kThreads;
     k_normal_pairs<<<grid, kThreads, 0, dev->stream>>>(reinterpret_cast<uint4*>(state), size, out, n, m, mean,
                                                         stddev);
