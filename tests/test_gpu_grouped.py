@@ -123,6 +123,7 @@ def test_grouped_bit_identical_to_single(gpu, vk, prec_name):
     # the single-problem path must not split K for a bit-for-bit comparison
     for s in specs:
         assert lib_.lib.vkc_gemm_tune_set(lib_.MM_BF16X3, s[2], s[3], s[4], 1) == 0
+        assert lib_.lib.vkc_gemm_tune_set(lib_.MM_FP32, s[2], s[3], s[4], 1) == 0
     try:
         fresh = [(ta, tb, M, N, K, a, b, A, B, vk.Array(gpu, data=np.zeros((M, N), np.float32)), bias, act, mask)
                  for (ta, tb, M, N, K, a, b, A, B, C0, bias, act, mask) in specs]
@@ -186,6 +187,7 @@ def test_grouped_sequence_matches_per_model_training(gpu, vk, prec):
     for (i, h, o, b) in dims:
         for (m, n, k) in ((b, h, i), (b, o, h), (o, h, b), (h, i, b), (b, h, o)):
             lib_.lib.vkc_gemm_tune_set(lib_.MM_BF16X3, m, n, k, 1)
+            lib_.lib.vkc_gemm_tune_set(lib_.MM_FP32, m, n, k, 1)
     try:
         ref = _models(vk, gpu, dims)
         ref_losses = []

@@ -1,6 +1,6 @@
 """
-Autotuner for the tensor-core GEMM (bf16 and split-bf16x3): CTA tile width
-and split-K count.
+Autotuner for the GEMMs: CTA tile width and split-K count of the tensor-core
+GEMM (bf16 and split-bf16x3), split-K count of the fp32 SIMT GEMM.
 
 For each size bucket (ceil(log2) of M, N and K) the tuner times every
 candidate (tile width 256 or 128, split count) on a representative problem of
@@ -45,7 +45,7 @@ def load_table(path: str = TABLE_PATH) -> int:
     with open(path) as f:
         data = json.load(f)
     n = 0
-    for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16)):
+    for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16), ("fp32", _lib.MM_FP32)):
         for entry in data.get(name, []):
             m, nn, k, splits = entry[:4]
             tile = int(entry[4]) if len(entry) > 4 else 256
@@ -126,8 +126,9 @@ def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) ->
     shapes = list(shapes or default_shapes())
     check(lib.vkc_gemm_tune_clear())
     table = {}
-    for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16)):
+    for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16), ("fp32", _lib.MM_FP32)):
         entries = []
+        tiles = TILES if prec != _lib.MM_FP32 else (256,)   # the SIMT GEMM has one tile shape
         for (m, n, k) in shapes:
             rng = np.random.default_rng(m * 31 + n * 7 + k)
             A = vk.Array(gpu, data=rng.standard_normal((m, k)).astype(np.float32))
@@ -136,7 +137,7 @@ def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) ->
             nk = (k + 63) // 64
             best, best_ms = (1, 256), float("inf")
             results = {}
-            for tile in TILES:
+            for tile in tiles:
                 for s in CANDIDATES:
                     if s > max(1, nk):
                         continue
@@ -162,7 +163,7 @@ def main():
     out = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else TABLE_PATH
     with open(out, "w") as f:
         json.dump(table, f, indent=1)
-    print(f"wrote {len(table['bf16x3'])} + {len(table['bf16'])} entries to {out}")
+    print(f"wrote {sum(len(table[k]) for k in ('bf16x3', 'bf16', 'fp32'))} entries to {out}")
 
 
 if __name__ == "__main__":

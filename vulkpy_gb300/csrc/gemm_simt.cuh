@@ -136,6 +136,26 @@ __device__ __forceinline__ void simt_tile(int64_t M, int64_t N, int64_t K, float
   }
 }
 
+// Split-K support (gemm_tc.cu): the fp32 split count from the tuning table
+// or heuristic, and the ordered reduction of the partial tiles with the
+// epilogue.
+int simt_splits(vkc_device_t dev, int64_t M, int64_t N, int64_t K);
+int gemm_splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M, int64_t N, float alpha,
+                       float beta, float* C, int64_t ldc, const GemmEpilogue& epi);
+
+// K range blockIdx.z of `span` into partial[z] (M x N, raw sums).
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(kGemmThreads)
+k_gemm_simt_split(int64_t M, int64_t N, int64_t K, const float* __restrict__ A, int64_t lda,
+                  const float* __restrict__ B, int64_t ldb, float* partial, int64_t span) {
+  __shared__ __align__(16) SimtSmem sm;
+  const int64_t k0 = (int64_t)blockIdx.z * span, kk = (K - k0 < span ? K - k0 : span);
+  const float* Az = A + (TA ? k0 * lda : k0);
+  const float* Bz = B + (TB ? k0 : k0 * ldb);
+  simt_tile<TA, TB>(M, N, kk, 1.0f, Az, lda, Bz, ldb, 0.0f, partial + (int64_t)blockIdx.z * M * N, N,
+                    GemmEpilogue{}, nullptr, (int64_t)blockIdx.y * kGemmBM, (int64_t)blockIdx.x * kGemmBN, sm);
+}
+
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(kGemmThreads)
 k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restrict__ A, int64_t lda,
@@ -173,6 +193,24 @@ inline int gemm_simt(vkc_device_t dev, bool ta, bool tb, int64_t M, int64_t N, i
   if (M == 0 || N == 0) return VKC_OK;
   dim3 grid((unsigned)((N + kGemmBN - 1) / kGemmBN), (unsigned)((M + kGemmBM - 1) / kGemmBM));
   VKC_REQUIRE(grid.y <= 65535, "matmul: M too large for the SIMT grid");
+  int splits = K > 0 ? simt_splits(dev, M, N, K) : 1;
+  if (splits > 1) {
+    // split K when the tiles cannot fill the GPU; partials added in split order
+    const int64_t span = (K + splits - 1) / splits;
+    splits = (int)((K + span - 1) / span);
+    float* partial = nullptr;
+    int r = scratch_alloc(dev, sizeof(float) * (size_t)splits * M * N, (void**)&partial);
+    if (r != VKC_OK) return r;
+    dim3 g3(grid.x, grid.y, (unsigned)splits);
+    if (!ta && !tb) k_gemm_simt_split<false, false><<<g3, kGemmThreads, 0, dev->stream>>>(M, N, K, A, lda, B, ldb, partial, span);
+    else if (ta && !tb) k_gemm_simt_split<true, false><<<g3, kGemmThreads, 0, dev->stream>>>(M, N, K, A, lda, B, ldb, partial, span);
+    else if (!ta && tb) k_gemm_simt_split<false, true><<<g3, kGemmThreads, 0, dev->stream>>>(M, N, K, A, lda, B, ldb, partial, span);
+    else k_gemm_simt_split<true, true><<<g3, kGemmThreads, 0, dev->stream>>>(M, N, K, A, lda, B, ldb, partial, span);
+    r = check_launch("gemm_simt split");
+    if (r == VKC_OK) r = gemm_splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
+    scratch_free(dev, partial);
+    return r;
+  }
   if (!ta && !tb) k_gemm_simt<false, false><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
   else if (ta && !tb) k_gemm_simt<true, false><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
   else if (!ta && tb) k_gemm_simt<false, true><<<grid, kGemmThreads, 0, dev->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);

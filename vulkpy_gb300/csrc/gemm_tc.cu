@@ -776,6 +776,29 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
 
 }  // namespace vkc
 
+namespace vkc {
+
+int gemm_splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M, int64_t N, float alpha,
+                       float beta, float* C, int64_t ldc, const GemmEpilogue& epi) {
+  return splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
+}
+
+// Split-K count of the fp32 SIMT GEMM (128 x 128 tiles): the tuning table's
+// fp32 entry, else split when the tiles cannot fill half the GPU.
+int simt_splits(vkc_device_t dev, int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = ((M + 127) / 128) * ((N + 127) / 128);
+  const int cap = (int)std::max<int64_t>(1, K / 64);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(VKC_MM_FP32, bucket(M), bucket(N), bucket(K)));
+    if (it != g_tune.end()) return std::max(1, std::min(it->second & 0xffff, cap));
+  }
+  if (tiles * 2 > dev->sm_count || K < 512) return 1;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(dev->sm_count / tiles, K / 256), 16));
+}
+
+}  // namespace vkc
+
 VKC_EXPORT int vkc_gemm_plan_set(int precision, int64_t m, int64_t n, int64_t k, int splits, int tile_n) {
   VKC_REQUIRE(splits >= 0 && splits <= 64, "splits out of range");
   VKC_REQUIRE(tile_n == 128 || tile_n == 256, "tile width must be 128 or 256");
@@ -793,6 +816,11 @@ VKC_EXPORT int vkc_gemm_tune_set(int precision, int64_t m, int64_t n, int64_t k,
 VKC_EXPORT int vkc_gemm_plan_get(vkc_device_t dev, int precision, int64_t m, int64_t n, int64_t k, int* splits,
                                  int* tile_n) {
   VKC_REQUIRE(dev && splits, "NULL argument");
+  if (precision == VKC_MM_FP32) {
+    *splits = vkc::simt_splits(dev, m, n, k);
+    if (tile_n) *tile_n = 128;
+    return VKC_OK;
+  }
   const vkc::TcPlan p = vkc::choose_plan(dev, precision, m, n, k);
   *splits = p.splits;
   if (tile_n) *tile_n = p.bn;
