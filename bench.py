@@ -172,6 +172,17 @@ def make_inputs(rows, cols, n_idx):
     return X, row, col, idx
 
 
+def max_over_ranks(x: float, dist) -> float:
+    """The largest value of `x` over all ranks (the slowest rank's time);
+    `x` itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
 def gpu_arm(args, rank, world, dist):
     import vulkpy_gb300 as vk
     from vulkpy_gb300 import _lib
@@ -214,11 +225,7 @@ def gpu_arm(args, rank, world, dist):
     clk = clocks.stop()
     bc_ms = [timer.ms(a, b) for a, b in spans]
     timer.free(t0, t1, *[j for s in spans for j in s])
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms_total], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t[0])
+    ms_total = max_over_ranks(ms_total, dist)
     ms_step = ms_total / args.steps
     value = world * nbytes / (ms_step * 1e-3) / 1e9
     launches = int(lc1.value - lc0.value)
@@ -336,12 +343,7 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     for _ in range(args.e2e_steps):
         one()
     gpu.wait()
-    dt = (time.perf_counter() - t0) / args.e2e_steps
-    if dist is not None:
-        import torch
-        t = torch.tensor([dt], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t[0])
+    dt = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, dist)
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, np.asarray)"}

@@ -13,8 +13,6 @@ Contents
   reference file:line each function follows).
 * :mod:`oracle.ops` -- numpy wrappers over the C library plus float64
   "truth" helpers used for error bounds.
-* :mod:`oracle.nn` -- float32 restatement of vulkpy's nn layers, losses and
-  optimizers in the reference's op order (vulkpy/nn/*.py).
 * :mod:`oracle.fake_vkarray` -- a numpy stand-in for vulkpy's native module
   ``_vkarray`` that lets the reference's own Python (vkarray.py, random.py,
   nn/) run on the CPU where the reference source is available; used only
