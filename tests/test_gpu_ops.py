@@ -324,3 +324,33 @@ def test_prng_segmented_streams(gpu, vk, size, n):
         got = np.asarray(r.normal(shape=(n // 2,), mean=0.5, stddev=3.0))
         np.testing.assert_allclose(got, ref.normal(n // 2, 0.5, 3.0), rtol=2e-6, atol=6e-6)
         np.testing.assert_array_equal(r.state().reshape(-1), ref.state)
+
+
+def test_pow_accuracy_wide_ranges(gpu, vk):
+    """pow (CUDA's powf) against float64: within its documented 4 ulp over
+    wide ranges, |x| near 1 with large |y|, negative x with integer y (sign
+    of odd powers), NaN for negative x with non-integer y, and the special
+    values (0, inf, NaN, overflow and underflow)."""
+    rng = np.random.default_rng(42)
+    n = 1 << 18
+    x = np.concatenate([
+        rng.uniform(-2, 2, n), np.exp(rng.uniform(-40, 40, n)), 1 + rng.uniform(-5e-3, 5e-3, n),
+        -rng.uniform(0.01, 10, n)]).astype(np.float32)
+    y = np.concatenate([
+        rng.uniform(0.5, 2, n), rng.uniform(-3, 3, n), rng.uniform(-2e4, 2e4, n),
+        rng.integers(-20, 21, n).astype(np.float64)]).astype(np.float32)
+    got = np.asarray(vk.Array(gpu, data=x) ** vk.Array(gpu, data=y))
+    with np.errstate(all="ignore"):
+        truth = np.power(x.astype(np.float64), y.astype(np.float64))
+    nan = np.isnan(truth)
+    np.testing.assert_array_equal(np.isnan(got), nan)
+    fin = ~nan & (np.abs(truth) < 3.4e38) & (np.abs(truth) > 1.2e-38)
+    assert O.ulp_distance(got[fin], truth[fin]).max() <= 4.0
+    over = ~nan & (np.abs(truth) >= 3.5e38)
+    assert np.all(np.isinf(got[over]) & (np.sign(got[over]) == np.sign(truth[over])))
+    sx = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 2.0, 2.0, 2.0, 0.5, 1.0], np.float32)
+    sy = np.array([2.0, 3.0, 0.5, 3.0, 1.0, np.inf, -np.inf, 0.0, 200.0, np.nan], np.float32)
+    gs = np.asarray(vk.Array(gpu, data=sx) ** vk.Array(gpu, data=sy))
+    with np.errstate(all="ignore"):
+        es = np.power(sx, sy)
+    np.testing.assert_array_equal(gs, es)
