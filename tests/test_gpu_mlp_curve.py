@@ -27,6 +27,8 @@ def _build():
 @pytest.mark.parametrize("prec,loss_tol,w_tol", [("fp32", 2e-4, 2e-3), ("bf16x3", 2e-3, 2e-2)])
 def test_loss_curve_matches_reference(gpu, prec, loss_tol, w_tol):
     import vulkpy_gb300 as vk
+    if not os.path.exists(FIXTURE):
+        pytest.skip("tests/golden/c4_loss_curve.npz not generated (tests/golden/make_c4_curve.py)")
     ref = np.load(FIXTURE)
     steps = int(ref["steps"][0])
     old = gpu.matmul_precision
