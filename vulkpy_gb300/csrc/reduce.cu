@@ -475,15 +475,13 @@ int reduce_axis_impl(vkc_device_t dev, const float* a, size_t prev, size_t axis,
     vkc::scratch_free(dev, partials);
     return r;
   }
-  // post > 1 (each thread keeps eight 16-byte rows in flight, so half the
-  // row-thread target fills HBM; fewer splits leave less to combine)
+  // post > 1
   const bool vec = (post % 4 == 0) && (((uintptr_t)a & 15u) == 0);
   const int vw = vec ? 4 : 1;
   const size_t cols_threads = prev * (post / vw);
-  const size_t col_target = vec ? target_threads / 2 : target_threads;
   int splits = 1;
-  if (cols_threads < col_target) {
-    size_t want = (col_target + cols_threads - 1) / cols_threads;
+  if (cols_threads < target_threads) {
+    size_t want = (target_threads + cols_threads - 1) / cols_threads;
     size_t maxs = std::max<size_t>(1, axis / 32);
     splits = (int)std::min<size_t>(std::min<size_t>(want, maxs), 65535);
   }
