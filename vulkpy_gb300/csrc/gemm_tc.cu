@@ -750,6 +750,10 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
     if (r != VKC_OK) return r;
   }
   const int64_t units = tiles * splits;
+  if (units >= (int64_t(1) << 31)) {
+    scratch_free(dev, partial);
+    return set_error(VKC_ERR_INVALID, "matmul: too many output tiles");
+  }
   const int clusters = (int)std::min<int64_t>(units, max_clusters(dev, kern, Cfg::kSmem));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * (unsigned)clusters, 1, 1);
