@@ -23,6 +23,7 @@ Differences in mechanism (the API and results follow the reference):
 from __future__ import annotations
 
 import ctypes as C
+import functools
 import logging
 import os
 import threading
@@ -613,7 +614,10 @@ class Array(_GPUArray):
             d = np.ascontiguousarray(np.asarray(data, dtype=np.float32))
             self._init_storage(d.shape, d)
         elif shape is not None:
-            self._init_storage(tuple(np.asarray(shape, dtype=int).reshape(-1)), None)
+            if type(shape) is tuple and all(type(v) is int for v in shape):
+                self._init_storage(shape, None)  # the common internal case, without numpy
+            else:
+                self._init_storage(tuple(int(v) for v in np.asarray(shape, dtype=int).reshape(-1)), None)
         else:
             raise ValueError("`data` or `shape` must not be `None`.")
 
@@ -640,12 +644,9 @@ class Array(_GPUArray):
             check(lib.vkc_binary(self._h, op, self._dptr(), other._dptr(), ret._buf.ptr or 0, self._size))
             ret._written()
             return ret
-        shape = tuple(np.broadcast_shapes(self.shape, other.shape))
+        shape, sa, sb, sc, nd = _bcast_plan(tuple(self.shape), tuple(other.shape))
         ret = self._new(shape)
-        nd = len(shape)
-        check(lib.vkc_broadcast_binary(
-            self._h, op, self._dptr(), shape_arg(_pad(self.shape, nd)), other._dptr(),
-            shape_arg(_pad(other.shape, nd)), ret._buf.ptr or 0, shape_arg(shape), nd))
+        check(lib.vkc_broadcast_binary(self._h, op, self._dptr(), sa, other._dptr(), sb, ret._buf.ptr or 0, sc, nd))
         ret._written()
         return ret
 
@@ -967,6 +968,16 @@ def matmul_grouped(a_list: Sequence["Array"], b_list: Sequence["Array"], precisi
     for c in outs:
         c._written()
     return outs
+
+
+@functools.lru_cache(maxsize=256)
+def _bcast_plan(a_shape: tuple, b_shape: tuple):
+    """Result shape and the C shape arguments of a broadcast binary op (the
+    ctypes arrays are read-only for the library, so one set per pair of
+    shapes serves every call)."""
+    shape = tuple(int(v) for v in np.broadcast_shapes(a_shape, b_shape))
+    nd = len(shape)
+    return shape, shape_arg(_pad(a_shape, nd)), shape_arg(_pad(b_shape, nd)), shape_arg(shape), nd
 
 
 def _pad(shape, nd) -> tuple:
