@@ -365,7 +365,7 @@ __device__ __forceinline__ void split_kmajor8_body(const float* __restrict__ src
     float x[8];
     if (k + 8 <= K) {
       const float4* p = reinterpret_cast<const float4*>(src + r * ld + k);
-      const float4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+      const float4 v0 = *p, v1 = *(p + 1);
       x[0] = v0.x, x[1] = v0.y, x[2] = v0.z, x[3] = v0.w, x[4] = v1.x, x[5] = v1.y, x[6] = v1.z, x[7] = v1.w;
     } else {
 #pragma unroll
@@ -406,7 +406,7 @@ __device__ __forceinline__ void split_transpose_body(const float* __restrict__ s
       if (k < K) {
         const float* p = src + k * ld + r;
         if (r + 3 < R) {
-          v = __ldcs(reinterpret_cast<const float4*>(p));
+          v = *reinterpret_cast<const float4*>(p);
         } else {
           if (r < R) v.x = p[0];
           if (r + 1 < R) v.y = p[1];

@@ -46,7 +46,7 @@ k_gemv_kcontig(int64_t J, int64_t K, float alpha, const float* __restrict__ P, i
       int64_t q = lane;
       for (; q + 96 < k4; q += 128) {  // four 16-byte loads in flight per lane
 #pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] = __ldcs(reinterpret_cast<const float4*>(row) + q + 32 * u);
+        for (int u = 0; u < 4; ++u) a[u] = *(reinterpret_cast<const float4*>(row) + q + 32 * u);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const float4 v = *(reinterpret_cast<const float4*>(vec) + q + 32 * u);
@@ -57,7 +57,7 @@ k_gemv_kcontig(int64_t J, int64_t K, float alpha, const float* __restrict__ P, i
         }
       }
       for (; q < k4; q += 32) {
-        const float4 m = __ldcs(reinterpret_cast<const float4*>(row) + q);
+        const float4 m = *(reinterpret_cast<const float4*>(row) + q);
         const float4 v = *(reinterpret_cast<const float4*>(vec) + q);
         s = fmaf(m.x, v.x, s);
         s = fmaf(m.y, v.y, s);
@@ -95,7 +95,7 @@ k_gemv_jcontig(int64_t J, int64_t K, float alpha, const float* __restrict__ P, i
       float v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        m[u] = __ldcs(reinterpret_cast<const float4*>(P + (k + u) * ld + j));
+        m[u] = *(reinterpret_cast<const float4*>(P + (k + u) * ld + j));
         v[u] = vec[(k + u) * vs];
       }
 #pragma unroll
@@ -107,7 +107,7 @@ k_gemv_jcontig(int64_t J, int64_t K, float alpha, const float* __restrict__ P, i
       }
     }
     for (; k < k1; ++k) {
-      const float4 m = __ldcs(reinterpret_cast<const float4*>(P + k * ld + j));
+      const float4 m = *(reinterpret_cast<const float4*>(P + k * ld + j));
       const float v = vec[k * vs];
       s0 = fmaf(m.x, v, s0);
       s1 = fmaf(m.y, v, s1);
@@ -160,7 +160,7 @@ k_gemv_jcontig8(int64_t J, int64_t K, float alpha, const float* __restrict__ P, 
       float v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        m[u] = __ldcs(reinterpret_cast<const float4*>(P + (k + u) * ld + j));
+        m[u] = *(reinterpret_cast<const float4*>(P + (k + u) * ld + j));
         v[u] = vec[(k + u) * vs];
       }
 #pragma unroll
@@ -172,7 +172,7 @@ k_gemv_jcontig8(int64_t J, int64_t K, float alpha, const float* __restrict__ P, 
       }
     }
     for (; k < a1; ++k) {
-      const float4 m = __ldcs(reinterpret_cast<const float4*>(P + k * ld + j));
+      const float4 m = *(reinterpret_cast<const float4*>(P + k * ld + j));
       const float v = vec[k * vs];
       s.x = fmaf(m.x, v, s.x);
       s.y = fmaf(m.y, v, s.y);
