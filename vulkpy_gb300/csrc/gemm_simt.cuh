@@ -2,7 +2,7 @@
 //
 // The plain-precision path of matmul.comp:23-33 (one invocation per output
 // with a serial K loop and uncoalesced B reads).  128x128 block tile, K
-// steps of 8, 256 threads each owning an 8x8 register tile split 4+4 in both
+// steps of 16, 256 threads each owning an 8x8 register tile split 4+4 in both
 // directions so shared-memory reads are conflict-free float4s; the next
 // K-step is prefetched into registers while the current one is multiplied
 // out of a double-buffered shared tile.  Within one output the K terms are
@@ -12,7 +12,7 @@
 
 namespace vkc {
 
-constexpr int kGemmBM = 128, kGemmBN = 128, kGemmBK = 8, kGemmThreads = 256;
+constexpr int kGemmBM = 128, kGemmBN = 128, kGemmBK = 16, kGemmThreads = 256;
 
 struct GemmEpilogue {
   const float* bias = nullptr;  // per output column, may be NULL
@@ -45,39 +45,68 @@ __device__ __forceinline__ void simt_tile(int64_t M, int64_t N, int64_t K, float
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
 
-  // Each thread loads 4 elements of the A tile and 4 of the B tile per K step.
+  // Per K step each thread loads 8 elements of the A tile and 8 of the B
+  // tile as two runs of 4 along the operand's contiguous index (one 16-byte
+  // load each when the run is inside the matrix and aligned).
   // op(A)(m,k) = TA ? A[k*lda + m] : A[m*lda + k]; op(B)(k,n) = TB ? B[n*ldb + k] : B[k*ldb + n].
-  float ra[4], rb[4];
+  const bool a_vec = (lda & 3) == 0 && (reinterpret_cast<uintptr_t>(A) & 15u) == 0;
+  const bool b_vec = (ldb & 3) == 0 && (reinterpret_cast<uintptr_t>(B) & 15u) == 0;
+  float4 ra[2], rb[2];
+  // run c of 512: contiguous along k -> (row c >> 2, k 4 (c & 3)); along m/n -> (4 (c & 31), k c >> 5)
+  auto load_run = [&](const float* P, int64_t ld, bool vec, bool kcontig, int64_t r0, int64_t R, int64_t k0,
+                      int c) -> float4 {
+    int64_t r, k;
+    if (kcontig) { r = r0 + (c >> 2); k = k0 + (c & 3) * 4; }
+    else { r = r0 + (c & 31) * 4; k = k0 + (c >> 5); }
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    float* pv = &v.x;
+    if (kcontig) {  // P[r*ld + k .. k+3]
+      if (r < R) {
+        if (vec && k + 3 < K) v = *reinterpret_cast<const float4*>(P + r * ld + k);
+        else
+#pragma unroll
+          for (int t = 0; t < 4; ++t) pv[t] = (k + t < K) ? P[r * ld + k + t] : 0.f;
+      }
+    } else {        // P[k*ld + r .. r+3]
+      if (k < K) {
+        if (vec && r + 3 < R) v = *reinterpret_cast<const float4*>(P + k * ld + r);
+        else
+#pragma unroll
+          for (int t = 0; t < 4; ++t) pv[t] = (r + t < R) ? P[k * ld + r + t] : 0.f;
+      }
+    }
+    return v;
+  };
   auto load_a = [&](int64_t k0) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      int e = tid + i * kGemmThreads;  // 0..1023 over (m: 128, k: 8)
-      int mm, kk;
-      if (TA) { mm = e & 127; kk = e >> 7; }   // contiguous along m
-      else { kk = e & 7; mm = e >> 3; }        // contiguous along k
-      int64_t gm = m0 + mm, gk = k0 + kk;
-      ra[i] = (gm < M && gk < K) ? (TA ? A[gk * lda + gm] : A[gm * lda + gk]) : 0.f;
-    }
+    for (int i = 0; i < 2; ++i) ra[i] = load_run(A, lda, a_vec, !TA, m0, M, k0, tid + i * kGemmThreads);
   };
   auto load_b = [&](int64_t k0) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      int e = tid + i * kGemmThreads;
-      int nn, kk;
-      if (TB) { kk = e & 7; nn = e >> 3; }     // contiguous along k
-      else { nn = e & 127; kk = e >> 7; }      // contiguous along n
-      int64_t gn = n0 + nn, gk = k0 + kk;
-      rb[i] = (gn < N && gk < K) ? (TB ? B[gn * ldb + gk] : B[gk * ldb + gn]) : 0.f;
-    }
+    for (int i = 0; i < 2; ++i) rb[i] = load_run(B, ldb, b_vec, TB, n0, N, k0, tid + i * kGemmThreads);
   };
   auto store = [&](int buf) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      int e = tid + i * kGemmThreads;
-      if (TA) As[buf][e >> 7][e & 127] = ra[i];
-      else As[buf][e & 7][e >> 3] = ra[i];
-      if (TB) Bs[buf][e & 7][e >> 3] = rb[i];
-      else Bs[buf][e >> 7][e & 127] = rb[i];
+    for (int i = 0; i < 2; ++i) {
+      const int c = tid + i * kGemmThreads;
+      if (!TA) {
+        const int mm = c >> 2, kq = (c & 3) * 4;
+        As[buf][kq][mm] = ra[i].x;
+        As[buf][kq + 1][mm] = ra[i].y;
+        As[buf][kq + 2][mm] = ra[i].z;
+        As[buf][kq + 3][mm] = ra[i].w;
+      } else {
+        *reinterpret_cast<float4*>(&As[buf][c >> 5][(c & 31) * 4]) = ra[i];
+      }
+      if (TB) {
+        const int nn = c >> 2, kq = (c & 3) * 4;
+        Bs[buf][kq][nn] = rb[i].x;
+        Bs[buf][kq + 1][nn] = rb[i].y;
+        Bs[buf][kq + 2][nn] = rb[i].z;
+        Bs[buf][kq + 3][nn] = rb[i].w;
+      } else {
+        *reinterpret_cast<float4*>(&Bs[buf][c >> 5][(c & 31) * 4]) = rb[i];
+      }
     }
   };
 
@@ -145,7 +174,7 @@ int gemm_splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64
 
 // K range blockIdx.z of `span` into partial[z] (M x N, raw sums).
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(kGemmThreads)
+__global__ void __launch_bounds__(kGemmThreads, 2)
 k_gemm_simt_split(int64_t M, int64_t N, int64_t K, const float* __restrict__ A, int64_t lda,
                   const float* __restrict__ B, int64_t ldb, float* partial, int64_t span) {
   __shared__ __align__(16) SimtSmem sm;
@@ -157,7 +186,7 @@ k_gemm_simt_split(int64_t M, int64_t N, int64_t K, const float* __restrict__ A, 
 }
 
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(kGemmThreads)
+__global__ void __launch_bounds__(kGemmThreads, 2)
 k_gemm_simt(int64_t M, int64_t N, int64_t K, float alpha, const float* __restrict__ A, int64_t lda,
             const float* __restrict__ B, int64_t ldb, float beta, float* C, int64_t ldc, GemmEpilogue epi) {
   __shared__ __align__(16) SimtSmem sm;

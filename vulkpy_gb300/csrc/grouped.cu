@@ -65,7 +65,7 @@ __device__ __forceinline__ int find_problem(const T* p, int count, int t) {
   return lo;
 }
 
-__global__ void __launch_bounds__(kGemmThreads) k_gemm_simt_grouped(const __grid_constant__ SimtTable tab) {
+__global__ void __launch_bounds__(kGemmThreads, 2) k_gemm_simt_grouped(const __grid_constant__ SimtTable tab) {
   __shared__ __align__(16) SimtSmem sm;
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
     const SimtProb& P = tab.p[find_problem(tab.p, tab.count, t)];
