@@ -81,7 +81,7 @@ def test_dense_layer_on_tensor_cores(gpu, vk):
 
 
 @pytest.mark.parametrize("m,n,k", [(256, 1024, 784), (64, 300, 2000), (1, 37, 4096), (385, 200, 130)])
-@pytest.mark.parametrize("prec,bound", [("bf16x3", 1e-5), ("bf16", 8e-3)])
+@pytest.mark.parametrize("prec,bound", [("bf16x3", 1e-5), ("bf16", 8e-3), ("fp32", 2e-6)])
 def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
     """Every plan the tuner may choose (tile width 256 or 128 x split count)
     gives the precision's accuracy, the table's choice is the one used, and a
@@ -90,7 +90,7 @@ def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
     the tile width)."""
     import ctypes as C
     from vulkpy_gb300 import _lib
-    P = {"bf16x3": _lib.MM_BF16X3, "bf16": _lib.MM_BF16}[prec]
+    P = {"bf16x3": _lib.MM_BF16X3, "bf16": _lib.MM_BF16, "fp32": _lib.MM_FP32}[prec]
     rng = np.random.default_rng(m + n + k)
     A = rng.standard_normal((m, k)).astype(np.float32)
     B = rng.standard_normal((n, k)).astype(np.float32)
@@ -103,7 +103,8 @@ def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
                 assert _lib.lib.vkc_gemm_plan_set(P, m, n, k, s, tile) == 0
                 got, got_tile = C.c_int(), C.c_int()
                 assert _lib.lib.vkc_gemm_plan_get(gpu.handle, P, m, n, k, C.byref(got), C.byref(got_tile)) == 0
-                assert got.value == min(s, (k + 63) // 64) and got_tile.value == tile
+                assert got.value == min(s, (k + 63) // 64)
+                assert got_tile.value == (128 if prec == "fp32" else tile)   # the SIMT GEMM has one tile
                 outs = []
                 for _ in range(2):
                     c = vk.Array(gpu, shape=(m, n))
@@ -116,7 +117,7 @@ def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
                 assert rel_fro(outs[0], exp) < bound, (tile, s)
                 if s == 1:
                     unsplit.append(outs[0])
-        np.testing.assert_array_equal(unsplit[0], unsplit[1])
+        np.testing.assert_array_equal(unsplit[0], unsplit[1])   # fp32: the same kernel twice
     finally:
         _lib.lib.vkc_gemm_tune_set(P, m, n, k, 0)
         from vulkpy_gb300 import autotune
