@@ -9,9 +9,11 @@ nn/models.py:55-78), one fixed batch of 256 N(0,1) rows with one-hot labels
 from integers(0, 10, 256); `steps` training steps.
 
 The reference's own Python (vulkpy/nn, vkarray.py, random.py) runs over the
-oracle's fake native module, about 3 s per step on 8 cores, so the default
-1000 steps take about an hour.  Run where the reference source tree exists:
-    python tests/golden/make_c4_curve.py [--steps 1000] [--reference PATH]
+oracle's fake native module, about 12 s per step on 8 cores (its Dense
+backward materialises a 256 x 1024 x 1024 array), so the committed fixture
+has the first 200 steps (about 40 minutes).  Run where the reference source
+tree exists:
+    python tests/golden/make_c4_curve.py [--steps 200] [--reference PATH]
 """
 from __future__ import annotations
 
@@ -49,7 +51,7 @@ def build(vk):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("VULKPY_REFERENCE_ROOT", "/root/reference"))
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--out", default=os.path.join(HERE, "c4_loss_curve.npz"))
     args = ap.parse_args()
     from oracle.fake_vkarray import load_reference

@@ -24,24 +24,26 @@ def _build():
     return mod.build
 
 
-@pytest.mark.parametrize("prec,loss_tol,w_tol", [("fp32", 2e-4, 2e-3), ("bf16x3", 2e-3, 2e-2)])
+# measured: fp32 2.4e-6 / 1.2e-5, split-bf16x3 4.0e-7 / 6.8e-6 (loss / last-layer weights)
+@pytest.mark.parametrize("prec,loss_tol,w_tol", [("fp32", 2e-5, 1e-4), ("bf16x3", 2e-5, 1e-4)])
 def test_loss_curve_matches_reference(gpu, prec, loss_tol, w_tol):
     import vulkpy_gb300 as vk
     if not os.path.exists(FIXTURE):
         pytest.skip("tests/golden/c4_loss_curve.npz not generated (tests/golden/make_c4_curve.py)")
     ref = np.load(FIXTURE)
     steps = int(ref["steps"][0])
-    old = gpu.matmul_precision
-    gpu.matmul_precision = prec
+    net, x, y = _build()(vk)
+    g = x._gpu                       # the workload opens its own GPU object
+    old = g.matmul_precision
+    g.matmul_precision = prec
     try:
-        net, x, y = _build()(vk)
         losses = np.empty(steps, np.float32)
         for i in range(steps):
             _, loss = net.train(x, y)
             losses[i] = np.asarray(loss).reshape(-1)[0]
         w_last = np.asarray(net.L[4].w.value).copy()
     finally:
-        gpu.matmul_precision = old
+        g.matmul_precision = old
     # the first step's loss depends only on the initial weights and the data
     np.testing.assert_allclose(losses[0], ref["loss"][0], rtol=1e-5)
     # then float32 summation orders differ (reference: serial sums; here: tiled
