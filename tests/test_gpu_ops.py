@@ -147,6 +147,15 @@ def test_broadcast_large_row_and_col(gpu, vk):
         fin = np.isfinite(truth)
         assert np.array_equal(np.isfinite(got), fin)
         assert O.ulp_distance(got[fin], truth[fin]).max() <= 3
+        # in place: the output is the first operand (full 4096-column chunks
+        # and the 4-column tail)
+        for op, meth in ((O.DIV, "__itruediv__"), (O.ADD, "__iadd__")):
+            z = vk.Array(gpu, data=X)
+            getattr(z, meth)(o)
+            np.testing.assert_array_equal(np.asarray(z), O.bcast(op, X, other))
+        z = vk.Array(gpu, data=np.abs(X) + 0.5)
+        z **= o
+        np.testing.assert_array_equal(np.asarray(z), np.asarray(vk.Array(gpu, data=np.abs(X) + 0.5) ** o))
 
 
 def test_clamp_variants(gpu, vk):
@@ -166,7 +175,8 @@ def test_clamp_variants(gpu, vk):
 
 SHAPES_AXES = [((7,), 0), ((513, 129), 0), ((513, 129), 1), ((3, 4100), 1), ((4100, 3), 0), ((2, 3, 4, 5), (1, 2)),
                ((2, 3, 4, 2, 2, 4, 3), (1, 2, 5)), ((64, 64, 64), (0, 2)), ((5, 70001), 1), ((70001, 2), 0),
-               ((1, 300000), 1), ((300000, 1), 0), ((9, 17), -1)]
+               ((1, 300000), 1), ((300000, 1), 0), ((9, 17), -1), ((512, 1024), 0), ((3, 700, 36), 1),
+               ((2100, 6), 0)]
 
 
 @pytest.mark.parametrize("shape,axis", SHAPES_AXES)
@@ -213,9 +223,10 @@ def test_full_reductions(gpu, vk, n):
     np.testing.assert_allclose(got, np.prod(p, dtype=np.float64), rtol=2e-5)
 
 
-def test_rebroadcast(gpu, vk):
+@pytest.mark.parametrize("shape", [(37, 300), (600, 64), (700, 30)])
+def test_rebroadcast(gpu, vk, shape):
     rng = np.random.default_rng(3)
-    a = rng.standard_normal((37, 300)).astype(np.float32)
+    a = rng.standard_normal(shape).astype(np.float32)
     x = vk.Array(gpu, data=a)
     for axis in (0, 1):
         got = np.asarray(x.maximum(axis=axis, rebroadcast=True))

@@ -432,6 +432,86 @@ k_cols(const float* a, size_t prev, size_t axis, size_t post, int splits, float*
   }
 }
 
+// post > 1, small inputs: one kernel instead of k_cols with axis slices
+// plus k_combine_splits (and their scratch).  A block of 32 warps owns
+// 32 x VW columns of one `prev` index; warp w walks axis slice w (the slices
+// k_cols would use with 32 splits), and the slices are merged in order
+// through shared memory, so the result equals that two-kernel path.
+constexpr int kColsBlockWarps = 32;
+// inputs up to 16 MiB take k_cols_block; larger ones stream through k_cols
+constexpr size_t kColsBlockMaxElems = size_t(1) << 22;
+
+template <int OP, bool COMP, int VW>
+__global__ void __launch_bounds__(kColsBlockWarps * 32)
+k_cols_block(const float* a, size_t prev, size_t axis, size_t post, float* out, int rebroadcast, float scale) {
+  __shared__ float sh_s[kColsBlockWarps][32 * VW], sh_c[kColsBlockWarps][32 * VW];
+  __shared__ float res[32 * VW];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const size_t ngroups = (post + 32 * VW - 1) / (32 * VW);
+  const size_t i = blockIdx.x / ngroups;
+  const size_t j = (blockIdx.x % ngroups) * 32 * VW + (size_t)lane * VW;
+  const bool cin = j < post;  // VW == 4 only when post % 4 == 0
+  const size_t span = (axis + kColsBlockWarps - 1) / kColsBlockWarps;
+  const size_t k0 = std::min(axis, (size_t)w * span), k1 = std::min(axis, k0 + span);
+  Acc<OP, COMP> acc[VW];
+#pragma unroll
+  for (int v = 0; v < VW; ++v) acc[v].init();
+  if (cin) {
+    const float* base = a + i * axis * post + j;
+    size_t k = k0;
+    if constexpr (VW == 4) {
+      for (; k + 7 < k1; k += 8) {
+        float4 x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = *reinterpret_cast<const float4*>(base + (k + u) * post);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          acc[0].push(x[u].x); acc[1].push(x[u].y); acc[2].push(x[u].z); acc[3].push(x[u].w);
+        }
+      }
+      for (; k < k1; ++k) {
+        const float4 x = *reinterpret_cast<const float4*>(base + k * post);
+        acc[0].push(x.x); acc[1].push(x.y); acc[2].push(x.z); acc[3].push(x.w);
+      }
+    } else {
+      for (; k + 7 < k1; k += 8) {
+        float x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = base[(k + u) * post];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[0].push(x[u]);
+      }
+      for (; k < k1; ++k) acc[0].push(base[k * post]);
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < VW; ++v) {
+    sh_s[w][lane * VW + v] = acc[v].s;
+    sh_c[w][lane * VW + v] = acc[v].c;
+  }
+  __syncthreads();
+  // warp v < VW merges column v of every lane, slices in order
+  if (w < VW) {
+    const int col = lane * VW + w;
+    Acc<OP, COMP> r;
+    r.init();
+    for (int ww = 0; ww < kColsBlockWarps; ++ww) r.merge(sh_s[ww][col], sh_c[ww][col]);
+    float val = r.value();
+    if (OP == VKC_SUM || OP == VKC_PROD) val *= scale;
+    res[col] = val;
+  }
+  __syncthreads();
+  if (!cin) return;
+  if (rebroadcast) {
+    for (size_t k = w; k < axis; k += kColsBlockWarps)
+#pragma unroll
+      for (int v = 0; v < VW; ++v) out[(i * axis + k) * post + j + v] = res[lane * VW + v];
+  } else if (w == 0) {
+#pragma unroll
+    for (int v = 0; v < VW; ++v) out[i * post + j + v] = res[lane * VW + v];
+  }
+}
+
 template <int OP, bool COMP>
 int reduce_axis_impl(vkc_device_t dev, const float* a, size_t prev, size_t axis, size_t post, float* out,
                      int rebroadcast, float scale) {
@@ -484,6 +564,21 @@ int reduce_axis_impl(vkc_device_t dev, const float* a, size_t prev, size_t axis,
     size_t want = (target_threads + cols_threads - 1) / cols_threads;
     size_t maxs = std::max<size_t>(1, axis / 32);
     splits = (int)std::min<size_t>(std::min<size_t>(want, maxs), 65535);
+  }
+  if (splits > 1 && prev * axis * post <= kColsBlockMaxElems) {
+    // 32 columns per block (scalar loads) unless 128-column blocks still
+    // cover every SM: the compensated sum's ~8 instructions per element
+    // would otherwise pile onto a few SMs
+    const bool vec4 = vec && prev * (post / 128) >= (size_t)dev->sm_count;
+    const size_t cols = vec4 ? 128 : 32;
+    const size_t blocks = prev * ((post + cols - 1) / cols);
+    if (vec4)
+      k_cols_block<OP, COMP, 4><<<(unsigned)blocks, kColsBlockWarps * 32, 0, dev->stream>>>(a, prev, axis, post, out,
+                                                                                        rebroadcast, scale);
+    else
+      k_cols_block<OP, COMP, 1><<<(unsigned)blocks, kColsBlockWarps * 32, 0, dev->stream>>>(a, prev, axis, post, out,
+                                                                                        rebroadcast, scale);
+    return vkc::check_launch("reduce_cols_block");
   }
   double* partials = nullptr;
   if (splits > 1) {
