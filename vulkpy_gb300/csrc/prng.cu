@@ -107,11 +107,32 @@ std::vector<uint32_t> powers(BitMatrix m, int K) {
   return out;
 }
 
+// Byte tables of the powers for the device: entry [k][p][v] = M^(2^k) applied
+// to byte value v placed at byte p of the state (bits 8p .. 8p+7), laid out
+// [K][16][256][4] words, so one application is 16 independent table loads
+// and xors (instead of one dependent load per set bit of the state).
+std::vector<uint32_t> byte_tables(const std::vector<uint32_t>& pows, int K) {
+  std::vector<uint32_t> out((size_t)K * 16 * 256 * 4, 0u);
+  for (int k = 0; k < K; ++k)
+    for (int p = 0; p < 16; ++p)
+      for (int v = 1; v < 256; ++v) {
+        // entry v = entry (v without its lowest bit) ^ column of that bit
+        const int low = __builtin_ctz((unsigned)v);
+        const uint32_t* prev = &out[(((size_t)k * 16 + p) * 256 + (v & (v - 1))) * 4];
+        const uint32_t* col = &pows[((size_t)k * 128 + p * 8 + low) * 4];
+        uint32_t* e = &out[(((size_t)k * 16 + p) * 256 + v) * 4];
+        for (int w = 0; w < 4; ++w) e[w] = prev[w] ^ col[w];
+      }
+  return out;
+}
+constexpr int kTableWords = 16 * 256 * 4;  // one power's byte tables
+
 constexpr int kJumpPowers = 32;  // states < 2^32
 
 int ensure_jump_powers(vkc_device_t dev) {
   if (dev->xo_jump_pows) return VKC_OK;
-  static std::vector<uint32_t> host_pows = powers(matrix_of([](uint32_t* s) { host_ref_jump(s); }), kJumpPowers);
+  static std::vector<uint32_t> host_pows =
+      byte_tables(powers(matrix_of([](uint32_t* s) { host_ref_jump(s); }), kJumpPowers), kJumpPowers);
   uint32_t* d = nullptr;
   VKC_CUDA(cudaMalloc(&d, host_pows.size() * sizeof(uint32_t)));
   cudaError_t e = cudaMemcpy(d, host_pows.data(), host_pows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -130,7 +151,8 @@ int ensure_jump_powers(vkc_device_t dev) {
 constexpr int kNextPowers = 48;  // up to 2^48 steps per state
 int ensure_next_powers(vkc_device_t dev) {
   if (dev->xo_next_pows) return VKC_OK;
-  static std::vector<uint32_t> host_pows = powers(matrix_of([](uint32_t* s) { host_step(s); }), kNextPowers);
+  static std::vector<uint32_t> host_pows =
+      byte_tables(powers(matrix_of([](uint32_t* s) { host_step(s); }), kNextPowers), kNextPowers);
   uint32_t* d = nullptr;
   VKC_CUDA(cudaMalloc(&d, host_pows.size() * sizeof(uint32_t)));
   cudaError_t e = cudaMemcpy(d, host_pows.data(), host_pows.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
@@ -171,21 +193,19 @@ __device__ __forceinline__ void box_muller(float u0, float u1, float mean, float
   z1 = __fmaf_rn(r, c, mean);
 }
 
-__device__ __forceinline__ uint4 apply_dev(const uint4* __restrict__ m, uint4 x) {
-  uint4 r = make_uint4(0, 0, 0, 0);
+// x times one power of a map, from its byte tables (16 x 256 entries).
+__device__ __forceinline__ uint4 apply_dev(const uint4* __restrict__ tab, uint4 x) {
   const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+  uint4 c[16];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    uint32_t bits = w[q];
-    while (bits) {
-      int b = __ffs(bits) - 1;
-      bits &= bits - 1;
-      uint4 c = __ldg(&m[q * 32 + b]);
-      r.x ^= c.x;
-      r.y ^= c.y;
-      r.z ^= c.z;
-      r.w ^= c.w;
-    }
+  for (int p = 0; p < 16; ++p) c[p] = __ldg(&tab[p * 256 + ((w[p >> 2] >> ((p & 3) * 8)) & 0xffu)]);
+  uint4 r = c[0];
+#pragma unroll
+  for (int p = 1; p < 16; ++p) {
+    r.x ^= c[p].x;
+    r.y ^= c[p].y;
+    r.z ^= c[p].z;
+    r.w ^= c[p].w;
   }
   return r;
 }
@@ -198,7 +218,7 @@ k_seed(uint4 s0, const uint4* __restrict__ jump_pows, uint32_t size, uint4* stat
   uint32_t e = i;
   int k = 0;
   while (e) {
-    if (e & 1u) x = apply_dev(jump_pows + (size_t)k * 128, x);
+    if (e & 1u) x = apply_dev(jump_pows + (size_t)k * (kTableWords / 4), x);
     e >>= 1;
     ++k;
   }
@@ -209,7 +229,7 @@ k_seed(uint4 s0, const uint4* __restrict__ jump_pows, uint32_t size, uint4* stat
 __device__ __forceinline__ uint4 advance(const uint4* __restrict__ pows, uint4 s, uint64_t e) {
   int k = 0;
   while (e) {
-    if (e & 1u) s = apply_dev(pows + (size_t)k * 128, s);
+    if (e & 1u) s = apply_dev(pows + (size_t)k * (kTableWords / 4), s);
     e >>= 1;
     ++k;
   }
@@ -328,9 +348,10 @@ k_box_muller(const float* u, float* out, size_t n, float mean, float stddev) {
 
 // Segments per state for `active` states of `steps` outputs each: enough
 // threads to fill the GPU, at least `min_len` steps per segment (a segment's
-// start costs one application of a power of N per set bit of its offset, so
-// cheap steps (uniform draws) need longer segments than Box-Muller pairs).
-// 1 = serial chains.
+// start costs one application of a power of N, 16 table loads, per set bit
+// of its offset, so cheap steps (uniform draws: 256) need longer segments
+// than Box-Muller pairs (16); 64 states x 65536 outputs: uniforms 24 -> 9 us,
+// normals 60 -> 19 us).  1 = serial chains.
 uint32_t segments(vkc_device_t dev, uint64_t active, uint64_t steps, uint64_t min_len) {
   const uint64_t want_threads = (uint64_t)dev->sm_count * 512;
   if (active >= want_threads || steps < 2 * min_len) return 1;
@@ -379,7 +400,7 @@ int generate(vkc_device_t dev, uint32_t* state, uint32_t size, void* out, size_t
   VKC_REQUIRE(((uintptr_t)state & 15u) == 0, "state buffer must be 16-byte aligned");
   uint32_t active = (uint32_t)std::min<size_t>(size, n);
   const uint64_t steps = (n + size - 1) / size;
-  const uint32_t G = segments(dev, active, steps, 1024);
+  const uint32_t G = segments(dev, active, steps, 256);
   if (G > 1) {
     const uint64_t L = (steps + G - 1) / G;
     return run_segmented(dev, state, active, [&](uint4* state_out, const uint4* pows) {
@@ -454,7 +475,7 @@ VKC_EXPORT int vkc_xoshiro_normal(vkc_device_t dev, uint32_t* state, uint32_t si
   if (size % 2 == 0) {
     uint32_t pairs = (uint32_t)std::min<size_t>(size / 2, m / 2);
     const uint64_t steps = (m + size - 1) / size;
-    const uint32_t G = segments(dev, pairs, steps, 64);
+    const uint32_t G = segments(dev, pairs, steps, 16);
     if (G > 1) {
       const uint64_t L = (steps + G - 1) / G;
       return run_segmented(dev, state, (uint32_t)std::min<size_t>(size, m), [&](uint4* state_out, const uint4* pows) {
