@@ -379,6 +379,16 @@ int vkc_dense_forward(vkc_device_t dev, int precision, const float* x, const flo
 int vkc_dense_backward(vkc_device_t dev, int precision, const float* x, const float* w,
                        const float* dy, float* dx, float* dw, float* db,
                        int64_t batch, int64_t in_dim, int64_t out_dim);
+/* An activation layer's backward followed by the preceding Dense layer's
+ * (nn/layers.py:158-267 then 104-141): dy = act'(y) * dy_act with the
+ * activation backward's float32 operations (act VKC_ACT_RELU or
+ * VKC_ACT_SIGMOID, y the activation output), stored in dy [batch, out_dim];
+ * then db += sum_b dy (rows in order), dW += dy^T x, dx = dy @ w (dx, dw, db
+ * may be NULL).  The activation backward and the bias sum share one launch;
+ * results equal vkc_activation_backward then vkc_dense_backward bit for bit. */
+int vkc_dense_backward_act(vkc_device_t dev, int precision, const float* x, const float* w,
+                           const float* dy_act, const float* y, int act, float* dy, float* dx,
+                           float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim);
 /* Row softmax over the last axis of [rows, cols] (nn/layers.py:297-300). */
 int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols);
 /* loss_rows[r] = sum_c -y log(p + 1e-8) with p = softmax(x) when softmax != 0

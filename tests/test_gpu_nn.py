@@ -121,14 +121,17 @@ def _params(net):
     return [np.asarray(p).copy() for L in net.L if hasattr(L, "w") for p in (L.w.value, L.b.value)]
 
 
+@pytest.mark.parametrize("batch", [32, 300])
 @pytest.mark.parametrize("prec", ["fp32", "bf16x3"])
-def test_fused_sequence_and_graph_replay_are_bit_identical(gpu, vk, prec):
-    """Dense+activation fusion and CUDA-graph replay change how many kernels
+def test_fused_sequence_and_graph_replay_are_bit_identical(gpu, vk, prec, batch):
+    """Dense+activation fusion (forward epilogue; backward activation
+    derivative + bias sum in one kernel, over one partial or a full and a
+    partial 256-row chunk) and CUDA-graph replay change how many kernels
     run, not the float32 results: parameters and losses match eager,
     unfused steps bit for bit."""
     rng = np.random.default_rng(0)
-    X = rng.standard_normal((32, 20)).astype(f32)
-    Y = np.eye(5, dtype=f32)[rng.integers(0, 5, 32)]
+    X = rng.standard_normal((batch, 20)).astype(f32)
+    Y = np.eye(5, dtype=f32)[rng.integers(0, 5, batch)]
     old = gpu.matmul_precision
     gpu.matmul_precision = prec
     try:

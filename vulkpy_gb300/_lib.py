@@ -117,6 +117,7 @@ _SIGS = {
     "vkc_xoshiro_randrange": ([vp, vp, u32, vp, sz, u32, u32], i32),
     "vkc_dense_forward": ([vp, i32, vp, vp, vp, vp, i64, i64, i64, i32], i32),
     "vkc_dense_backward": ([vp, i32, vp, vp, vp, vp, vp, vp, i64, i64, i64], i32),
+    "vkc_dense_backward_act": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64], i32),
     "vkc_softmax": ([vp, vp, vp, i64, i64], i32),
     "vkc_cross_entropy": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
     "vkc_adam_update": ([vp, vp, vp, vp, vp, sz, f64, f64, f64, f64, f64, f64], i32),

@@ -6,7 +6,7 @@
 // has only a few loads in flight and waits on memory latency for every few
 // rows; here the block stages 256-row chunks of its 32 columns in shared
 // memory (each of the 8 warps loads 32 rows: 32 coalesced 128-byte loads in
-// flight per thread) and warp 0 then adds each column from shared memory in
+// flight per warp) and warp 0 then adds each column from shared memory in
 // row order.
 #pragma once
 #include <cstdint>
@@ -26,11 +26,20 @@ __device__ __forceinline__ float colsum32(const float* __restrict__ y, int64_t r
   float s = 0.f;
   for (int64_t r0 = 0; r0 < rows; r0 += kColsumRows) {
     const int n = (int)(rows - r0 < kColsumRows ? rows - r0 : kColsumRows);
+    if (n == kColsumRows) {
+      // a full chunk: the warp's 32 row loads all in flight at once
+      float v[kColsumRows / 8];
+#pragma unroll
+      for (int q = 0; q < kColsumRows / 8; ++q) v[q] = in ? y[(r0 + w + 8 * q) * ld + c0 + lane] : 0.f;
+#pragma unroll
+      for (int q = 0; q < kColsumRows / 8; ++q) tile[w + 8 * q][lane] = v[q];
+    } else {
 #pragma unroll 8
-    for (int r = w; r < n; r += 8) tile[r][lane] = in ? y[(r0 + r) * ld + c0 + lane] : 0.f;
+      for (int r = w; r < n; r += 8) tile[r][lane] = in ? y[(r0 + r) * ld + c0 + lane] : 0.f;
+    }
     __syncthreads();
     if (w == 0) {
-#pragma unroll 16
+#pragma unroll 32
       for (int r = 0; r < n; ++r) s += tile[r][lane];
     }
     __syncthreads();

@@ -521,7 +521,13 @@ __global__ void __launch_bounds__(256) k_fill_grouped(const __grid_constant__ Ve
     const VecItem& I = tab.it[find_vec(tab, t)];
     const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
     const int64_t i1 = min(i0 + kVecChunk, I.n);
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) I.value[i] = I.scale;
+    if ((reinterpret_cast<uintptr_t>(I.value) & 15u) == 0 && i1 - i0 == kVecChunk) {
+      const float4 f = make_float4(I.scale, I.scale, I.scale, I.scale);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) *reinterpret_cast<float4*>(I.value + i0 + (int64_t)(u * 256 + threadIdx.x) * 4) = f;
+    } else {
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) I.value[i] = I.scale;
+    }
   }
 }
 
@@ -545,6 +551,19 @@ struct AdamTable {
   AdamItem it[kMaxGroup];
 };
 
+// One element of the Adam update, the float32 operations of the
+// single-tensor kernel in the same order.
+__device__ __forceinline__ void adam_elem(const AdamTable& tab, float d1, float d2, float gi, float& mi, float& vi,
+                                          float& xi) {
+  mi = __fadd_rn(__fmul_rn(mi, tab.b1), __fmul_rn(tab.c1, gi));
+  vi = __fadd_rn(__fmul_rn(vi, tab.b2), __fmul_rn(tab.c2, __fmul_rn(gi, gi)));
+  float mhat = __fdiv_rn(mi, d1);
+  const float vhat = __fadd_rn(__fsqrt_rn(__fdiv_rn(vi, d2)), tab.eps);
+  mhat = __fmul_rn(mhat, tab.nlr);
+  mhat = __fdiv_rn(mhat, vhat);
+  xi = __fadd_rn(xi, mhat);
+}
+
 __global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ AdamTable tab) {
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
     int lo = 0, hi = tab.count - 1;
@@ -558,17 +577,40 @@ __global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ Ad
     const float d1 = (float)(1.0 - p1), d2 = (float)(1.0 - p2);
     const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
     const int64_t i1 = min(i0 + kVecChunk, I.n);
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) {
-      const float gi = I.grad[i];
-      float mi = __fadd_rn(__fmul_rn(I.m[i], tab.b1), __fmul_rn(tab.c1, gi));
-      float vi = __fadd_rn(__fmul_rn(I.v[i], tab.b2), __fmul_rn(tab.c2, __fmul_rn(gi, gi)));
-      I.m[i] = mi;
-      I.v[i] = vi;
-      float mhat = __fdiv_rn(mi, d1);
-      float vhat = __fadd_rn(__fsqrt_rn(__fdiv_rn(vi, d2)), tab.eps);
-      mhat = __fmul_rn(mhat, tab.nlr);
-      mhat = __fdiv_rn(mhat, vhat);
-      I.value[i] = __fadd_rn(I.value[i], mhat);
+    const bool vec = ((reinterpret_cast<uintptr_t>(I.value) | reinterpret_cast<uintptr_t>(I.grad) |
+                       reinterpret_cast<uintptr_t>(I.m) | reinterpret_cast<uintptr_t>(I.v)) & 15u) == 0;
+    if (vec && i1 - i0 == kVecChunk) {
+      // a full chunk: 4 float4 of each array per thread, every load issued
+      // before the first store (the four arrays are distinct, but the
+      // compiler cannot know it)
+      float4 gg[4], mm[4], vv[4], xx[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + (int64_t)(u * 256 + threadIdx.x) * 4;
+        gg[u] = *reinterpret_cast<const float4*>(I.grad + i);
+        mm[u] = *reinterpret_cast<const float4*>(I.m + i);
+        vv[u] = *reinterpret_cast<const float4*>(I.v + i);
+        xx[u] = *reinterpret_cast<const float4*>(I.value + i);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + (int64_t)(u * 256 + threadIdx.x) * 4;
+        adam_elem(tab, d1, d2, gg[u].x, mm[u].x, vv[u].x, xx[u].x);
+        adam_elem(tab, d1, d2, gg[u].y, mm[u].y, vv[u].y, xx[u].y);
+        adam_elem(tab, d1, d2, gg[u].z, mm[u].z, vv[u].z, xx[u].z);
+        adam_elem(tab, d1, d2, gg[u].w, mm[u].w, vv[u].w, xx[u].w);
+        *reinterpret_cast<float4*>(I.m + i) = mm[u];
+        *reinterpret_cast<float4*>(I.v + i) = vv[u];
+        *reinterpret_cast<float4*>(I.value + i) = xx[u];
+      }
+    } else {
+      for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) {
+        float mi = I.m[i], vi = I.v[i], xi = I.value[i];
+        adam_elem(tab, d1, d2, I.grad[i], mi, vi, xi);
+        I.m[i] = mi;
+        I.v[i] = vi;
+        I.value[i] = xi;
+      }
     }
     __syncthreads();  // this chunk has read the powers
     if (threadIdx.x == 0) {

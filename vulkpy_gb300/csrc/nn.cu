@@ -34,6 +34,23 @@ int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64
   return vkc::set_error(VKC_ERR_INVALID, "unknown matmul precision %d", precision);
 }
 
+// dW[out,in] += dy[B,out]^T @ x[B,in] and dx[B,in] = dy[B,out] @ W[out,in]
+// (either may be NULL).
+int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy, float* dx,
+                         float* dw, int64_t batch, int64_t in_dim, int64_t out_dim) {
+  int r = VKC_OK;
+  if (dw) {
+    r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw, in_dim,
+                 vkc::GemmEpilogue{});
+    if (r != VKC_OK) return r;
+  }
+  if (dx) {
+    r = gemm_any(dev, precision, false, false, batch, in_dim, out_dim, 1.0f, dy, out_dim, w, in_dim, 0.0f, dx, in_dim,
+                 vkc::GemmEpilogue{});
+  }
+  return r;
+}
+
 // db[o] += sum_b dy[b, o], b in order (one block per 32 columns).
 __global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
   __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
@@ -180,19 +197,66 @@ k_adam_dev(float* value, const float* grad, float* m, float* v, size_t n, float 
 
 // ReLU: dx = max(sign(y), 0) * dy; Sigmoid / Softmax diagonal: ((1 - y) * y) * dy.
 template <int ACT>
+__device__ __forceinline__ float act_bwd(float yi, float dyi) {
+  if (ACT == VKC_ACT_RELU) {
+    float s = yi > 0.f ? 1.f : (yi < 0.f ? -1.f : yi);
+    s = fmaxf(s, 0.f);
+    return __fmul_rn(s, dyi);
+  } else {
+    return __fmul_rn(__fmul_rn(__fsub_rn(1.0f, yi), yi), dyi);
+  }
+}
+
+template <int ACT>
 __global__ void __launch_bounds__(kThreads)
 k_act_backward(const float* y, const float* dy, float* dx, size_t n) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const float yi = y[i];
-    if (ACT == VKC_ACT_RELU) {
-      float s = yi > 0.f ? 1.f : (yi < 0.f ? -1.f : yi);
-      s = fmaxf(s, 0.f);
-      dx[i] = __fmul_rn(s, dy[i]);
-    } else {
-      dx[i] = __fmul_rn(__fmul_rn(__fsub_rn(1.0f, yi), yi), dy[i]);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dx[i] = act_bwd<ACT>(y[i], dy[i]);
+}
+
+// An activation's backward fused with the next Dense layer's bias gradient:
+// dy = act'(y) * dy_act (k_act_backward's float32 operations) is stored for
+// the weight and input GEMMs and, in the same block, summed over the batch
+// in row order (k_colsum_acc's arithmetic): one launch instead of two, and dy
+// is not read back for db.  One block per 32 columns, 256-row chunks staged
+// in shared memory; each thread issues its 2 x 32 loads before its stores.
+template <int ACT>
+__global__ void __launch_bounds__(256) k_act_colsum(const float* y, const float* dy_act, float* dy, int64_t batch,
+                                                    int64_t out_dim, float* db) {
+  __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
+  constexpr int kQ = vkc::kColsumRows / 8;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t c = (int64_t)blockIdx.x * vkc::kColsumCols + lane;
+  const bool in = c < out_dim;
+  float s = 0.f;
+  for (int64_t r0 = 0; r0 < batch; r0 += vkc::kColsumRows) {
+    const int n = (int)(batch - r0 < vkc::kColsumRows ? batch - r0 : vkc::kColsumRows);
+    float yv[kQ], gv[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+      const int r = w + 8 * q;
+      const bool ok = in && r < n;
+      const int64_t off = (r0 + r) * out_dim + c;
+      yv[q] = ok ? y[off] : 0.f;
+      gv[q] = ok ? dy_act[off] : 0.f;
     }
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) {
+      const int r = w + 8 * q;
+      if (r < n) {
+        const float v = act_bwd<ACT>(yv[q], gv[q]);
+        if (in) dy[(r0 + r) * out_dim + c] = v;
+        tile[r][lane] = v;
+      }
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll 32
+      for (int r = 0; r < n; ++r) s += tile[r][lane];
+    }
+    __syncthreads();
   }
+  if (db && w == 0 && in) db[c] += s;
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -259,24 +323,33 @@ VKC_EXPORT int vkc_dense_backward(vkc_device_t dev, int precision, const float* 
   if (batch == 0) return VKC_OK;
   VKC_REQUIRE(x && w && dy, "NULL buffer");
   int r = VKC_OK;
-  if (db) {
+  if (db && out_dim > 0) {
     unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
     k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db);
     r = vkc::check_launch("dense_backward db");
     if (r != VKC_OK) return r;
   }
-  if (dw) {
-    // dW[out,in] += dy[B,out]^T @ x[B,in]
-    r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw, in_dim,
-                 vkc::GemmEpilogue{});
+  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, batch, in_dim, out_dim);
+}
+
+VKC_EXPORT int vkc_dense_backward_act(vkc_device_t dev, int precision, const float* x, const float* w,
+                                      const float* dy_act, const float* y, int act, float* dy, float* dx, float* dw,
+                                      float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
+  if (batch == 0) return VKC_OK;
+  VKC_REQUIRE(x && w && dy_act && y && dy, "NULL buffer");
+  VKC_REQUIRE(act == VKC_ACT_RELU || act == VKC_ACT_SIGMOID, "activation %d has no backward kernel", act);
+  if (out_dim > 0) {
+    const unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
+    if (act == VKC_ACT_RELU)
+      k_act_colsum<VKC_ACT_RELU><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db);
+    else
+      k_act_colsum<VKC_ACT_SIGMOID><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db);
+    const int r = vkc::check_launch("dense_backward_act dy, db");
     if (r != VKC_OK) return r;
   }
-  if (dx) {
-    // dx[B,in] = dy[B,out] @ W[out,in]
-    r = gemm_any(dev, precision, false, false, batch, in_dim, out_dim, 1.0f, dy, out_dim, w, in_dim, 0.0f, dx, in_dim,
-                 vkc::GemmEpilogue{});
-  }
-  return r;
+  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, batch, in_dim, out_dim);
 }
 
 VKC_EXPORT int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols) {

@@ -3,7 +3,9 @@ Layers (vulkpy/nn/layers.py:18-323).
 
 Dense runs one fused GEMM+bias kernel forward and two GEMMs plus a column
 sum backward, accumulating straight into the parameter gradients (the
-reference builds a (batch, out, in) product and sums it, layers.py:131-135).
+reference builds a (batch, out, in) product and sums it, layers.py:131-135);
+``backward_act`` also takes the following activation's backward into the
+column-sum kernel.
 Softmax forward is one fused kernel per row.  The backward formulas are the
 reference's, including Softmax's diagonal-only gradient dy*y*(1-y)
 (layers.py:302-323), kept for drop-in parity.
@@ -64,6 +66,31 @@ class Dense(Module):
             dy._h, _PREC[dy._gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy._dptr(),
             dx._buf.ptr if dx is not None else None, wg._dptr() if wg is not None else None,
             bg._dptr() if bg is not None else None, dy.shape[0], self.input_dim, self.output_dim))
+        if wg is not None:
+            wg._written()
+        if bg is not None:
+            bg._written()
+        if dx is not None:
+            dx._written()
+        return dx
+
+    def backward_act(self, dy_act: Array, act: int, y: Array, need_dx: bool = True) -> Array:
+        """The backward of the activation that follows this layer (output
+        ``y``, gradient ``dy_act``) and then this layer's backward, with the
+        activation derivative and the bias gradient in one kernel; the same
+        float32 results as the two ``backward`` calls."""
+        x = self._x
+        gpu = dy_act._gpu
+        dy = Array(gpu, shape=(dy_act.shape[0], self.output_dim))
+        dx = Array(gpu, shape=(dy_act.shape[0], self.input_dim)) if need_dx else None
+        wg = self.w.grad
+        bg = self.b.grad
+        check(lib.vkc_dense_backward_act(
+            dy_act._h, _PREC[gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy_act._dptr(), y._dptr(),
+            act, dy._buf.ptr or 0, dx._buf.ptr if dx is not None else None,
+            wg._dptr() if wg is not None else None, bg._dptr() if bg is not None else None,
+            dy_act.shape[0], self.input_dim, self.output_dim))
+        dy._written()
         if wg is not None:
             wg._written()
         if bg is not None:

@@ -21,8 +21,9 @@ class Sequence:
     Execution differs from the reference only in how many kernels run, not
     in the float32 results: a Dense followed by ReLU or Sigmoid runs as one
     GEMM with the activation in its epilogue (the Dense pre-activation output
-    is then not kept as ``dense._y``), and the first layer's input gradient,
-    which nothing consumes, is not computed.
+    is then not kept as ``dense._y``), backward the activation derivative
+    and that Dense's bias gradient share one kernel, and the first layer's
+    input gradient, which nothing consumes, is not computed.
 
     Like the reference, parameter regularizers are not applied by ``train``
     (vulkpy's Sequence never calls ``regular_grad``); pass
@@ -58,12 +59,22 @@ class Sequence:
 
     def _backward(self):
         dx = self.loss.grad()
-        for k in range(len(self.L) - 1, -1, -1):
+        k = len(self.L) - 1
+        while k >= 0:
             layer = self.L[k]
+            prev = self.L[k - 1] if k >= 1 else None
+            if (self.fuse and type(layer) in (ReLU, Sigmoid) and type(prev) is Dense
+                    and getattr(layer, "_y", None) is not None
+                    and len(dx.shape) == 2):
+                # the activation's backward and the Dense bias sum in one kernel
+                dx = prev.backward_act(dx, layer.act, layer._y, need_dx=k - 1 > 0)
+                k -= 2
+                continue
             if k == 0 and isinstance(layer, Dense):
                 layer.backward(dx, need_dx=False)
             else:
                 dx = layer.backward(dx)
+            k -= 1
 
     def _params(self):
         """The trainable Parameters of the Dense layers, or None when another
