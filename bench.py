@@ -300,6 +300,7 @@ def profile_ops(vk, gpu, timer, X, row, col, idx, rng, U, Nrm, I):
     timed("bcast_row", 8 * n, lambda: X + row)
     timed("bcast_col", 8 * n, lambda: X * col)
     Z = timed("unary_abs", 8 * n, lambda: X.abs())
+    Z += 1e-3  # log on |X| + 1e-3, as in the step
     timed("unary_log", 8 * n, lambda: Z.log())
     timed("scalar_mul", 8 * n, lambda: X * 1e-4)
     timed("sum_axis0", 4 * n, lambda: X.sum(axis=0))
