@@ -393,7 +393,7 @@ class _GPUArray(Resource):
     def _init_storage(self, shape, data: Optional[np.ndarray]):
         self.shape = tuple(int(s) for s in shape)
         self._size = _prod(self.shape)
-        nbytes = self._size * np.dtype(self._dtype).itemsize
+        nbytes = self._size * 4  # float32 and uint32 elements
         self._buf = _DevBuf(self._gpu._dev, nbytes, data)
 
     # -- synchronisation
@@ -595,14 +595,20 @@ class Shape(U32Array):
 
 
 def _normalize_axes(axis, ndim) -> List[int]:
-    axes = np.unique(np.asarray(axis, dtype=np.int64).reshape(-1))
-    out = []
+    """Distinct axes in [0, ndim), descending; a plain int or a tuple/list of
+    ints skips numpy (this runs on every axis reduction)."""
+    if isinstance(axis, (int, np.integer)):
+        axes = (int(axis),)
+    elif isinstance(axis, (tuple, list)) and all(isinstance(a, (int, np.integer)) for a in axis):
+        axes = tuple(int(a) for a in axis)
+    else:
+        axes = tuple(int(a) for a in np.asarray(axis, dtype=np.int64).reshape(-1))
+    out = set()
     for a in axes:
-        a = int(a)
         if a < -ndim or a >= ndim:
             raise ValueError(f"axis {a} is out of bounds for array of dimension {ndim}")
-        out.append(a % ndim)
-    return sorted(set(out), reverse=True)
+        out.add(a % ndim)
+    return sorted(out, reverse=True)
 
 
 class Array(_GPUArray):
