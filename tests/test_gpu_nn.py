@@ -216,16 +216,20 @@ def test_branches_in_a_graph_match_sequential_eager(gpu, vk):
             np.testing.assert_array_equal(pa, pb)
 
 
+@pytest.mark.parametrize("hidden", [16, 130])
 @pytest.mark.parametrize("optname", ["adam", "sgd"])
-def test_grouped_parameter_update_matches_per_parameter(gpu, vk, optname):
+def test_grouped_parameter_update_matches_per_parameter(gpu, vk, optname, hidden):
     """A Sequence whose parameters share one optimizer zeroes every gradient
     and updates every parameter in one launch each; a copy whose layers have
     their own optimizer objects (same hyperparameters) takes the
     per-parameter path.  Parameters, moments and the device-side Adam powers
-    match bit for bit, eager and replayed from a captured step."""
+    match bit for bit, eager and replayed from a captured step.  Hidden width
+    130 gives a 64 x 130 weight (two full 4096-element chunks, the 128-bit
+    path, plus a ragged tail)."""
     nn = vk.nn
     rng = np.random.default_rng(4)
-    X = rng.standard_normal((24, 12)).astype(f32)
+    n_in = 12 if hidden == 16 else 64
+    X = rng.standard_normal((24, n_in)).astype(f32)
     Y = np.eye(3, dtype=f32)[rng.integers(0, 3, 24)]
 
     def make(shared):
@@ -233,9 +237,9 @@ def test_grouped_parameter_update_matches_per_parameter(gpu, vk, optname):
         o = mk()
         opts = [o if shared else mk() for _ in range(4)]
         return nn.Sequence([
-            nn.Dense(gpu, 12, 16, w_opt=opts[0], b_opt=opts[1], w_init=nn.HeNormal(gpu, 12, seed=3)),
+            nn.Dense(gpu, n_in, hidden, w_opt=opts[0], b_opt=opts[1], w_init=nn.HeNormal(gpu, n_in, seed=3)),
             nn.ReLU(),
-            nn.Dense(gpu, 16, 3, w_opt=opts[2], b_opt=opts[3], w_init=nn.HeNormal(gpu, 16, seed=4)),
+            nn.Dense(gpu, hidden, 3, w_opt=opts[2], b_opt=opts[3], w_init=nn.HeNormal(gpu, hidden, seed=4)),
         ], nn.SoftmaxCrossEntropyLoss())
 
     per, grouped, graphed = make(False), make(True), make(True)
