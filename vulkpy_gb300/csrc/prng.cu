@@ -277,7 +277,18 @@ k_generate(uint4* state, uint32_t size, void* out, size_t n, uint32_t low, uint3
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= size || (size_t)t >= n) return;
   uint4 s = state[t];
-  for (size_t k = t; k < n; k += size) put<MODE>(out, k, next(s), low, range);
+  const size_t step = size;
+  const size_t cnt = (n - t + step - 1) / step;  // outputs of state t
+  size_t k = t, j = 0;
+  // four draws, then their four stores
+  for (; j + 4 <= cnt; j += 4, k += 4 * step) {
+    const uint32_t r0 = next(s), r1 = next(s), r2 = next(s), r3 = next(s);
+    put<MODE>(out, k, r0, low, range);
+    put<MODE>(out, k + step, r1, low, range);
+    put<MODE>(out, k + 2 * step, r2, low, range);
+    put<MODE>(out, k + 3 * step, r3, low, range);
+  }
+  for (; j < cnt; ++j, k += step) put<MODE>(out, k, next(s), low, range);
   state[t] = s;
 }
 
