@@ -103,7 +103,8 @@ def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
                 assert _lib.lib.vkc_gemm_plan_set(P, m, n, k, s, tile) == 0
                 got, got_tile = C.c_int(), C.c_int()
                 assert _lib.lib.vkc_gemm_plan_get(gpu.handle, P, m, n, k, C.byref(got), C.byref(got_tile)) == 0
-                assert got.value == min(s, (k + 63) // 64)
+                kstep = 16 if prec == "fp32" else 64   # SIMT K step / tensor-core K block
+                assert got.value == min(s, (k + kstep - 1) // kstep)
                 assert got_tile.value == (128 if prec == "fp32" else tile)   # the SIMT GEMM has one tile
                 outs = []
                 for _ in range(2):

@@ -10,7 +10,7 @@ time is a table lookup: deterministic, the same in eager runs and graph
 captures.  Buckets without an entry fall back to an occupancy heuristic.
 
 Run on the GPU:
-    python -c "import vulkpy_gb300.autotune as t; t.main()" [--quick] [--out FILE]
+    python -c "import vulkpy_gb300.autotune as t; t.main()" [--quick] [--only fp32] [--out FILE]
 """
 from __future__ import annotations
 
@@ -120,13 +120,15 @@ def _time_gemm(gpu, a, b, c, m, n, k, reps=5, calls=16, prec=None) -> float:
     return float(np.median(times))
 
 
-def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) -> dict:
+def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True, only: str = None) -> dict:
     import vulkpy_gb300 as vk
     gpu = vk.GPU()
     shapes = list(shapes or default_shapes())
     check(lib.vkc_gemm_tune_clear())
     table = {}
     for name, prec in (("bf16x3", _lib.MM_BF16X3), ("bf16", _lib.MM_BF16), ("fp32", _lib.MM_FP32)):
+        if only is not None and name != only:
+            continue
         entries = []
         tiles = TILES if prec != _lib.MM_FP32 else (256,)   # the SIMT GEMM has one tile shape
         for (m, n, k) in shapes:
@@ -134,7 +136,7 @@ def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) ->
             A = vk.Array(gpu, data=rng.standard_normal((m, k)).astype(np.float32))
             B = vk.Array(gpu, data=rng.standard_normal((n, k)).astype(np.float32))
             Cm = vk.Array(gpu, shape=(m, n))
-            nk = (k + 63) // 64
+            nk = (k + 15) // 16 if prec == _lib.MM_FP32 else (k + 63) // 64   # K steps / K blocks
             best, best_ms = (1, 256), float("inf")
             results = {}
             for tile in tiles:
@@ -159,8 +161,17 @@ def tune(shapes: Iterable[Tuple[int, int, int]] = None, verbose: bool = True) ->
 
 
 def main():
-    table = tune(default_shapes()[:12] if "--quick" in sys.argv else None)
+    """``--only NAME`` re-tunes one precision (bf16x3, bf16 or fp32) and keeps
+    the other precisions' entries of the existing table."""
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    table = tune(default_shapes()[:12] if "--quick" in sys.argv else None, only=only)
     out = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else TABLE_PATH
+    if only is not None and os.path.exists(TABLE_PATH):
+        with open(TABLE_PATH) as f:
+            old = json.load(f)
+        for name in ("bf16x3", "bf16", "fp32"):
+            if name != only:
+                table[name] = old.get(name, [])
     with open(out, "w") as f:
         json.dump(table, f, indent=1)
     print(f"wrote {sum(len(table[k]) for k in ('bf16x3', 'bf16', 'fp32'))} entries to {out}")

@@ -791,7 +791,9 @@ int gemm_splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64
 // fp32 entry, else split when the tiles cannot fill half the GPU.
 int simt_splits(vkc_device_t dev, int64_t M, int64_t N, int64_t K) {
   const int64_t tiles = ((M + 127) / 128) * ((N + 127) / 128);
-  const int cap = (int)std::max<int64_t>(1, (K + 63) / 64);  // K ranges of at least 64 (as the tensor-core plans)
+  // K ranges of at least one 16-deep K step of the SIMT tile (small GEMMs
+  // gain from many splits: 256^3 with 16 ranges 12.3 -> 9.0 us)
+  const int cap = (int)std::max<int64_t>(1, (K + kGemmBK - 1) / kGemmBK);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(tune_key(VKC_MM_FP32, bucket(M), bucket(N), bucket(K)));
