@@ -22,6 +22,8 @@ struct vkc_device {
   cudaStream_t stream = nullptr;       // current compute stream (own or user's)
   cudaStream_t copy_stream = nullptr;  // uploads into fresh buffers
   cudaEvent_t copy_done = nullptr;     // reused marker for uploads
+  cudaStream_t side_stream = nullptr;  // independent work forked from `stream` inside one call
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   uint32_t* err_word = nullptr;        // device error flags (bit0: gather index)
   uint32_t* xo_jump_pows = nullptr;    // xoshiro jump-map powers (lazy)
   uint32_t* xo_next_pows = nullptr;    // xoshiro next-map powers (lazy)

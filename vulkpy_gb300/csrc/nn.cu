@@ -35,9 +35,32 @@ int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64
 }
 
 // dW[out,in] += dy[B,out]^T @ x[B,in] and dx[B,in] = dy[B,out] @ W[out,in]
-// (either may be NULL).
+// (either may be NULL).  With both, the weight GEMM runs on the device's
+// side stream, forked from the current stream and joined back before
+// returning, so the two independent GEMMs (and their operand splits and
+// split-K reductions) overlap; inside a graph capture they become parallel
+// branches.  Each GEMM's own arithmetic is unchanged, so results are too.
+// Only from the device's own stream: on a branch's or a caller's stream the
+// one side stream would tie independent branches together.
 int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy, float* dx,
                          float* dw, int64_t batch, int64_t in_dim, int64_t out_dim) {
+  if (dw && dx && dev->side_stream && dev->stream == dev->own_stream) {
+    cudaStream_t main = dev->stream;
+    VKC_CUDA(cudaEventRecord(dev->side_fork, main));
+    VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->side_fork, 0));
+    dev->stream = dev->side_stream;
+    int r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw,
+                     in_dim, vkc::GemmEpilogue{});
+    dev->stream = main;
+    // the join is recorded even after an error, so a capture stays joined
+    cudaError_t e = cudaEventRecord(dev->side_join, dev->side_stream);
+    if (r == VKC_OK)
+      r = gemm_any(dev, precision, false, false, batch, in_dim, out_dim, 1.0f, dy, out_dim, w, in_dim, 0.0f, dx,
+                   in_dim, vkc::GemmEpilogue{});
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(main, dev->side_join, 0);
+    if (e != cudaSuccess && r == VKC_OK) r = vkc::set_error(VKC_ERR_CUDA, "side stream join: %s", cudaGetErrorString(e));
+    return r;
+  }
   int r = VKC_OK;
   if (dw) {
     r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw, in_dim,

@@ -139,6 +139,9 @@ VKC_EXPORT int vkc_device_open(int index, float priority, vkc_device_t* out) {
   e = cudaStreamCreateWithPriority(&dev->own_stream, cudaStreamNonBlocking, prio);
   if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->copy_stream, cudaStreamNonBlocking, prio);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->copy_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->side_stream, cudaStreamNonBlocking, prio);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->side_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->side_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&dev->err_word, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemset(dev->err_word, 0, sizeof(uint32_t));
   if (e != cudaSuccess) {
@@ -168,9 +171,13 @@ VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
   if (dev->err_word) cudaFree(dev->err_word);
   if (dev->xo_jump_pows) cudaFree(dev->xo_jump_pows);
   if (dev->xo_next_pows) cudaFree(dev->xo_next_pows);
+  cudaStreamSynchronize(dev->side_stream);
   cudaEventDestroy(dev->copy_done);
+  cudaEventDestroy(dev->side_fork);
+  cudaEventDestroy(dev->side_join);
   cudaStreamDestroy(dev->own_stream);
   cudaStreamDestroy(dev->copy_stream);
+  cudaStreamDestroy(dev->side_stream);
   delete dev;
   return VKC_OK;
 }
