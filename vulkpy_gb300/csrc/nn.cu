@@ -34,23 +34,41 @@ int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64
   return vkc::set_error(VKC_ERR_INVALID, "unknown matmul precision %d", precision);
 }
 
-// dW[out,in] += dy[B,out]^T @ x[B,in] and dx[B,in] = dy[B,out] @ W[out,in]
-// (either may be NULL).  With both, the weight GEMM runs on the device's
-// side stream, forked from the current stream and joined back before
+// db[o] += sum_b dy[b, o], b in order (one block per 32 columns).
+__global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
+  __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
+  const int64_t c0 = (int64_t)blockIdx.x * vkc::kColsumCols;
+  const float s = vkc::colsum32(dy, batch, out_dim, out_dim, c0, tile);
+  const int64_t o = c0 + threadIdx.x;
+  if (threadIdx.x < 32 && o < out_dim) db[o] += s;
+}
+
+// db[o] += sum_b dy[b, o], dW[out,in] += dy[B,out]^T @ x[B,in] and
+// dx[B,in] = dy[B,out] @ W[out,in] (any may be NULL).  With dW and dx, the
+// bias sum and the weight GEMM run on the device's side stream, forked from the current stream and joined back before
 // returning, so the two independent GEMMs (and their operand splits and
 // split-K reductions) overlap; inside a graph capture they become parallel
 // branches.  Each GEMM's own arithmetic is unchanged, so results are too.
 // Only from the device's own stream: on a branch's or a caller's stream the
 // one side stream would tie independent branches together.
+int colsum_into(vkc_device_t dev, const float* dy, float* db, int64_t batch, int64_t out_dim) {
+  if (!db || out_dim <= 0) return VKC_OK;
+  const unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
+  k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db);
+  return vkc::check_launch("dense_backward db");
+}
+
 int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy, float* dx,
-                         float* dw, int64_t batch, int64_t in_dim, int64_t out_dim) {
+                         float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
   if (dw && dx && dev->side_stream && dev->stream == dev->own_stream) {
     cudaStream_t main = dev->stream;
     VKC_CUDA(cudaEventRecord(dev->side_fork, main));
     VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->side_fork, 0));
     dev->stream = dev->side_stream;
-    int r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw,
-                     in_dim, vkc::GemmEpilogue{});
+    int r = colsum_into(dev, dy, db, batch, out_dim);
+    if (r == VKC_OK)
+      r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw,
+                   in_dim, vkc::GemmEpilogue{});
     dev->stream = main;
     // the join is recorded even after an error, so a capture stays joined
     cudaError_t e = cudaEventRecord(dev->side_join, dev->side_stream);
@@ -61,7 +79,8 @@ int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const 
     if (e != cudaSuccess && r == VKC_OK) r = vkc::set_error(VKC_ERR_CUDA, "side stream join: %s", cudaGetErrorString(e));
     return r;
   }
-  int r = VKC_OK;
+  int r = colsum_into(dev, dy, db, batch, out_dim);
+  if (r != VKC_OK) return r;
   if (dw) {
     r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw, in_dim,
                  vkc::GemmEpilogue{});
@@ -72,15 +91,6 @@ int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const 
                  vkc::GemmEpilogue{});
   }
   return r;
-}
-
-// db[o] += sum_b dy[b, o], b in order (one block per 32 columns).
-__global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
-  __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
-  const int64_t c0 = (int64_t)blockIdx.x * vkc::kColsumCols;
-  const float s = vkc::colsum32(dy, batch, out_dim, out_dim, c0, tile);
-  const int64_t o = c0 + threadIdx.x;
-  if (threadIdx.x < 32 && o < out_dim) db[o] += s;
 }
 
 __device__ __forceinline__ float warp_max(float v) {
@@ -345,14 +355,7 @@ VKC_EXPORT int vkc_dense_backward(vkc_device_t dev, int precision, const float* 
   VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
   if (batch == 0) return VKC_OK;
   VKC_REQUIRE(x && w && dy, "NULL buffer");
-  int r = VKC_OK;
-  if (db && out_dim > 0) {
-    unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
-    k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db);
-    r = vkc::check_launch("dense_backward db");
-    if (r != VKC_OK) return r;
-  }
-  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, batch, in_dim, out_dim);
+  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, db, batch, in_dim, out_dim);
 }
 
 VKC_EXPORT int vkc_dense_backward_act(vkc_device_t dev, int precision, const float* x, const float* w,
@@ -372,7 +375,7 @@ VKC_EXPORT int vkc_dense_backward_act(vkc_device_t dev, int precision, const flo
     const int r = vkc::check_launch("dense_backward_act dy, db");
     if (r != VKC_OK) return r;
   }
-  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, batch, in_dim, out_dim);
+  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, nullptr, batch, in_dim, out_dim);
 }
 
 VKC_EXPORT int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols) {
