@@ -8,11 +8,11 @@
 // keeps ~16 significant bits per operand (relative representation error
 // <= 2^-17) at three tensor-core products instead of fp32 FMA.
 //
-// k_gemm_tcp is persistent (one CTA per SM, 2-CTA clusters sharing the op(B)
-// tile through TMA multicast) with two TMEM accumulators, so a tile's
-// epilogue overlaps the next tile's MMAs.  Every mbarrier wait is bounded by
-// a wall-clock limit; on expiry the CTA records bit1 in the device error
-// word, drains what it issued and returns.
+// k_gemm_tcp is persistent (one CTA per SM; each CTA loads every operand tile
+// it multiplies into its own shared memory) with two TMEM accumulators, so a
+// tile's epilogue overlaps the next tile's MMAs.  Every mbarrier wait is
+// bounded by a wall-clock limit; on expiry the CTA records bit1 in the device
+// error word, drains what it issued and returns.
 #include "gemm_tc.cuh"
 #include "tc_ptx.cuh"
 #include "tc_epilogue.cuh"
@@ -29,15 +29,15 @@ namespace vkc {
 namespace {
 
 // ------------------------------------------------------------ the kernel
-// Persistent, cluster-paired tensor-core GEMM.
+// Persistent tensor-core GEMM.
 //
-// Work unit: a 256 x 256 block of C (two 128-row tiles, one per CTA of a
-// 2-CTA cluster) over one K range (split K).  The two CTAs of a cluster walk
-// the same unit sequence in lockstep; each loads its own 128 rows of op(A)
-// and one 128-row half of the shared op(B) tile, multicast to both CTAs, so
-// every CTA reads 32 KB (bf16) or 64 KB (split) from L2 per 64-wide K block
-// instead of 48 / 96 KB.  Each CTA computes its 128 x 256 tile with
-// single-CTA tcgen05.mma (M=128, N=256, K=16) into one of two 256-column TMEM
+// Work unit: a 128 x BN tile of C over one K range (split K).  CTA b takes
+// units b, b + grid, ...; units run through the tiles in raster groups of 16
+// tile rows (down a column of tiles first), so the CTAs working at the same
+// time multiply the same few op(B) tiles and the repeated reads hit L2.  Each
+// CTA TMA-loads its 128 rows of op(A) and the whole op(B) tile into its own
+// shared memory (no clusters; CTAs share nothing) and computes its tile with
+// single-CTA tcgen05.mma (M=128, N=BN, K=16) into one of two TMEM
 // accumulators, so the epilogue of one accumulation overlaps the MMAs of the
 // next.
 //
@@ -51,14 +51,13 @@ namespace {
 // tensor pipe's truncating accumulation spans at most DRAIN*64 of K.
 constexpr int kEpiWarps = 8;
 constexpr int kThreadsP = 32 * (2 + kEpiWarps);
-constexpr int kGroupM = 8;         // cluster rows per raster group (L2 reuse)
+constexpr int kGroupM = 16;        // tile rows per raster group (L2 reuse)
 
 
 // BN: columns of C per CTA tile (256 or 128; the autotuner picks per shape).
 template <bool X3, int BN, int STAGES>
 struct PCfg {
   static constexpr uint32_t kABytes = kBM * kBK * 2;             // 16 KB
-  static constexpr uint32_t kBHalf = (BN / 2) * kBK * 2;         // one CTA's half of the B tile
   static constexpr uint32_t kBBytes = BN * kBK * 2;
   static constexpr uint32_t kStageBytes = (X3 ? 2u : 1u) * (kABytes + kBBytes);
   static constexpr uint32_t kBarOff = STAGES * kStageBytes;
@@ -73,15 +72,15 @@ struct PUnit {
 };
 
 template <int BN>
-__device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int m_pairs, int n_blocks, int rank) {
+__device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int m_blocks, int n_blocks) {
   const int tile = u / splits, z = u - tile * splits;
   const int per_group = kGroupM * n_blocks;
   const int g = tile / per_group, first = g * kGroupM;
-  const int gsize = min(kGroupM, m_pairs - first);
+  const int gsize = min(kGroupM, m_blocks - first);
   const int within = tile - g * per_group;
-  const int mp = first + within % gsize, nb = within / gsize;
+  const int mb = first + within % gsize, nb = within / gsize;
   PUnit p;
-  p.m0 = (2 * mp + rank) * kBM;
+  p.m0 = mb * kBM;
   p.n0 = nb * BN;
   p.kb0 = z * kps;
   p.nkb = max(0, min(nk, p.kb0 + kps) - p.kb0);
@@ -94,7 +93,7 @@ __global__ void __launch_bounds__(kThreadsP, 1)
 k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
            const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
            int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-           uint32_t* err, float* __restrict__ partial, int splits, int kps, int m_pairs, int n_blocks) {
+           uint32_t* err, float* __restrict__ partial, int splits, int kps, int m_blocks, int n_blocks) {
   using Cfg = PCfg<X3, BN, STAGES>;
   constexpr uint32_t kCols = 2 * BN;  // two accumulators
   constexpr int CW = BN / 2;          // columns per epilogue warp
@@ -112,15 +111,14 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rank = (int)cluster_ctarank();
-  const int cluster = blockIdx.x >> 1, nclusters = gridDim.x >> 1;
+
   const int nk = (K + kBK - 1) / kBK;
-  const int units = m_pairs * n_blocks * splits;
+  const int units = m_blocks * n_blocks * splits;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(full_bar(s), 1);
-      mbar_init(empty_bar(s), 2);  // one commit from each CTA's MMA issuer
+      mbar_init(empty_bar(s), 1);  // the MMA issuer's commit
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(accf_bar(b), 1);
@@ -137,9 +135,7 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
-  // the peer multicasts into this CTA's stages and barriers: both CTAs'
-  // barriers must be initialised before either producer starts
-  cluster_sync_all();
+  __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
 
@@ -158,19 +154,18 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     }
     int it = 0;
     bool ok = true;
-    for (int u = cluster; u < units && ok; u += nclusters) {
-      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_pairs, n_blocks, rank);
-      const int nb_row = p.n0 + (BN / 2) * rank;
+    for (int u = (int)blockIdx.x; u < units && ok; u += (int)gridDim.x) {
+      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_blocks, n_blocks);
       for (int kb = 0; kb < p.nkb; ++kb, ++it) {
         const int s = it % STAGES;
         if (*abort_flag || !mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1)) { ok = false; break; }
         mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
         const int kx = (p.kb0 + kb) * kBK;
         tma_load_2d(stage_a(s), &map_a, full_bar(s), kx, p.m0);
-        tma_load_2d_mc(stage_b(s) + rank * Cfg::kBHalf, &map_b, full_bar(s), kx, nb_row, 3);
+        tma_load_2d(stage_b(s), &map_b, full_bar(s), kx, p.n0);
         if (X3) {
           tma_load_2d(stage_alo(s), &map_alo, full_bar(s), kx, p.m0);
-          tma_load_2d_mc(stage_blo(s) + rank * Cfg::kBHalf, &map_blo, full_bar(s), kx, nb_row, 3);
+          tma_load_2d(stage_blo(s), &map_blo, full_bar(s), kx, p.n0);
         }
       }
     }
@@ -178,8 +173,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
       atomicOr(err, 2u);
       *abort_flag = 1;
     }
-    // Tail: wait until both CTAs' MMAs have released every stage, so no
-    // commit from the peer is still in flight towards this CTA at exit.
+    // Tail: wait until the MMAs have released every stage, so no copy or
+    // commit is still in flight at exit.
     for (int t = 0; t < STAGES && it - STAGES + t >= 0; ++t) {
       const int j = it - STAGES + t;
       if (!mbar_wait(empty_bar(j % STAGES), (j / STAGES) & 1)) {
@@ -195,8 +190,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
                                | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
     int it = 0, acc_it = 0;
     bool ok = true;
-    for (int u = cluster; u < units && ok; u += nclusters) {
-      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_pairs, n_blocks, rank);
+    for (int u = (int)blockIdx.x; u < units && ok; u += (int)gridDim.x) {
+      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_blocks, n_blocks);
       const int span = X3 ? DRAIN : p.nkb;  // K blocks per accumulation
       for (int g0 = 0; g0 < p.nkb && ok; g0 += span, ++acc_it) {
         const int b = acc_it & 1;
@@ -222,7 +217,7 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
               mma_bf16(d, a, bb, idesc, first);
             }
           }
-          mma_commit_mc(empty_bar(s), 3);  // frees stage s in both CTAs once read
+          mma_commit(empty_bar(s));  // frees stage s once read
         }
         if (!ok) break;
         mma_commit(accf_bar(b));
@@ -243,8 +238,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
     int acc_it = 0;
     bool ok = true;
-    for (int u = cluster; u < units && ok; u += nclusters) {
-      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_pairs, n_blocks, rank);
+    for (int u = (int)blockIdx.x; u < units && ok; u += (int)gridDim.x) {
+      const PUnit p = unit_of<BN>(u, splits, kps, nk, m_blocks, n_blocks);
       const int span = X3 ? DRAIN : p.nkb;
       const int ngroups = (p.nkb + span - 1) / span;
       float acc[X3 ? CW : 1];
@@ -326,8 +321,6 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
   }
-  // neither CTA leaves while the other may still signal or fill its memory
-  cluster_sync_all();
 }
 
 // ------------------------------------------------------------ operand split
@@ -601,10 +594,9 @@ struct TcPlan {
   int splits;  // K ranges
 };
 
-// CTA tiles (128 x bn) of an M x N problem, counting the idle partner of an
-// odd last row of tiles (the 2-CTA clusters pair tile rows).
+// CTA tiles (128 x bn) of an M x N problem.
 inline int64_t cta_tiles(int64_t M, int64_t N, int bn) {
-  return 2 * (((M + kBM - 1) / kBM + 1) / 2) * ((N + bn - 1) / bn);
+  return ((M + kBM - 1) / kBM) * ((N + bn - 1) / bn);
 }
 
 TcPlan choose_plan(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_t K) {
@@ -700,29 +692,19 @@ int splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M,
   return check_launch("splitk_reduce");
 }
 
-// Clusters of this kernel that fit on the device at once (cached).
+// Resident CTAs of this kernel on the device (cached per instantiation).
 template <class Kern>
-int max_clusters(vkc_device_t dev, Kern kern, uint32_t smem) {
+int max_ctas(vkc_device_t dev, Kern kern, uint32_t smem) {
   static int cached = 0;
   if (cached > 0) return cached;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(2 * (unsigned)dev->sm_count, 1, 1);
-  cfg.blockDim = dim3(kThreadsP, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = 2;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg) != cudaSuccess || n <= 0) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)kern, kThreadsP, smem) != cudaSuccess ||
+      per_sm <= 0) {
     cudaGetLastError();
-    n = dev->sm_count / 2;
+    per_sm = 1;
   }
-  cached = n;
-  return n;
+  cached = per_sm * dev->sm_count;
+  return cached;
 }
 
 template <bool X3, int BN, int STAGES, int DRAIN>
@@ -737,9 +719,8 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
     attr_set = true;
   }
   const int64_t m_blocks = (M + kBM - 1) / kBM;
-  const int m_pairs = (int)((m_blocks + 1) / 2);
   const int n_blocks = (int)((N + BN - 1) / BN);
-  const int64_t tiles = (int64_t)m_pairs * n_blocks;
+  const int64_t tiles = m_blocks * n_blocks;
   const int nk = (int)((K + kBK - 1) / kBK);
   // no empty split
   const int kps = (nk + splits - 1) / splits;
@@ -754,23 +735,11 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
     scratch_free(dev, partial);
     return set_error(VKC_ERR_INVALID, "matmul: too many output tiles");
   }
-  const int clusters = (int)std::min<int64_t>(units, max_clusters(dev, kern, Cfg::kSmem));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(2 * (unsigned)clusters, 1, 1);
-  cfg.blockDim = dim3(kThreadsP, 1, 1);
-  cfg.dynamicSmemBytes = Cfg::kSmem;
-  cfg.stream = dev->stream;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = 2;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc,
-                                     epi.bias, epi.act, dev->err_word, partial, splits, kps, m_pairs, n_blocks);
-  int r = e == cudaSuccess ? check_launch("gemm_tc") : set_error(VKC_ERR_CUDA, "gemm_tc launch: %s",
-                                                                  cudaGetErrorString(e));
+  const int ctas = (int)std::min<int64_t>(units, max_ctas(dev, kern, Cfg::kSmem));
+  kern<<<(unsigned)ctas, kThreadsP, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta,
+                                                                 C, ldc, epi.bias, epi.act, dev->err_word, partial,
+                                                                 splits, kps, (int)m_blocks, n_blocks);
+  int r = check_launch("gemm_tc");
   if (r == VKC_OK && splits > 1) r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
   scratch_free(dev, partial);
   return r;
@@ -869,14 +838,14 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   // op(A)(m,k): ta ? A[k*lda + m] : A[m*lda + k]  -> K contiguous iff !ta
   // op(B)(k,n): tb ? B[n*ldb + k] : B[k*ldb + n]  -> (n,k) K contiguous iff tb
   r = split_operands(dev, A, M, lda, !ta, a_hi, a_lo, B, N, ldb, tb, b_hi, b_lo, K, Kp);
-  // boxes are 64 K wide: 128 rows for a CTA's op(A) tile, bn/2 rows for
-  // one CTA's half of the op(B) tile
+  // boxes are 64 K wide: 128 rows for a CTA's op(A) tile, bn rows for its
+  // op(B) tile
   const TcPlan plan = choose_plan(dev, precision, M, N, K);
   CUtensorMap ma, mb, malo, mblo;
   if (r == VKC_OK) r = make_map(&ma, a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, plan.bn / 2);
+  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, plan.bn);
   if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, plan.bn / 2);
+  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, plan.bn);
   if (r == VKC_OK) {
     // stages fill ~192 KB of shared memory
     if (x3 && plan.bn == 256)

@@ -149,45 +149,6 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 }  // namespace
 }  // namespace vkc
 
-// ------------------------------------------------------------ cluster helpers
-namespace vkc {
-namespace {
-
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-// All threads of every CTA in the cluster: release this CTA's prior shared
-// memory writes (barrier inits) to the cluster and wait for the others.
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-// 2-D TMA load delivered to the same shared-memory offset (and completing on
-// the mbarrier at the same offset) in every CTA of `mask`.
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar), "h"(mask)
-      : "memory");
-}
-
-// Arrive (once) on the mbarrier at offset `bar` of every CTA in `mask` when
-// all tcgen05 operations issued so far by this thread have completed.
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
-      "h"(mask)
-      : "memory");
-}
-
-}  // namespace
-}  // namespace vkc
-
 namespace vkc {
 namespace {
 
