@@ -319,38 +319,58 @@ def profile_ops(vk, gpu, timer, X, row, col, idx, rng, U, Nrm, I):
 def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, dist):
     """Same step through the public API from pinned host buffers: uploads of
     X, row, col, idx and read-back of the reductions and the final X are
-    inside the timed region."""
-    Xp = vk.vkarray.empty_pinned(Xh.shape)
-    Xp[...] = Xh
-    idxp = vk.vkarray.empty_pinned(idxh.shape, np.uint32)
-    idxp[...] = idxh
-    h2d = Xp.nbytes + rowh.nbytes + colh.nbytes + idxp.nbytes
+    inside the timed region, every step.  Pipelined as a user would write
+    it: step i's results start copying back (``prefetch``) as soon as its ops
+    are issued, step i+1's uploads and ops are issued next, and only then
+    does the host read step i's results -- so step i's read-back and step
+    i+1's upload overlap the compute instead of adding to it."""
+    pins = []
+    for h in (Xh, rowh, colh, idxh):
+        p_ = vk.vkarray.empty_pinned(h.shape, h.dtype)
+        p_[...] = h
+        pins.append(p_)
+    Xp, rowp, colp, idxp = pins
+    h2d = sum(p_.nbytes for p_ in pins)
     d2h = 0
 
-    def one():
-        nonlocal d2h
+    def issue():
         X = vk.Array(gpu, data=Xp)
-        row, col = vk.Array(gpu, data=rowh), vk.Array(gpu, data=colh)
+        row, col = vk.Array(gpu, data=rowp), vk.Array(gpu, data=colp)
         idx = vk.U32Array(gpu, data=idxp)
         outs, g = run_step(vk, X, row, col, idx, rng, U, Nrm, I)
+        for o in outs:
+            o.prefetch()
+        X.prefetch()
+        return outs, X
+
+    def collect(pending):
+        nonlocal d2h
+        outs, X = pending
         got = [np.asarray(o) for o in outs]
         final = np.asarray(X)
         d2h = sum(o.nbytes for o in got) + final.nbytes
-        return final
 
-    for _ in range(max(1, args.warmup)):
-        one()
+    def run(steps):
+        pending = None
+        for _ in range(steps):
+            cur = issue()
+            if pending is not None:
+                collect(pending)
+            pending = cur
+        collect(pending)
+
+    run(max(1, args.warmup))
     gpu.wait()
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        one()
+    run(args.e2e_steps)
     gpu.wait()
     dt = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, dist)
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-            "api": "vulkpy_gb300 public API (Array(data=pinned), ops, np.asarray)"}
+            "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
+                   "step i+1 issued before step i's results are read"}
 
 
 # ---------------------------------------------------------------- matmul / MLP

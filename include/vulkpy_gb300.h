@@ -74,6 +74,10 @@ enum vkc_matmul_precision {
 /* activation fused into the Dense epilogue */
 enum vkc_activation { VKC_ACT_NONE = 0, VKC_ACT_RELU = 1, VKC_ACT_SIGMOID = 2 };
 
+/* losses (vulkpy/nn/losses.py): CrossEntropyLoss, SoftmaxCrossEntropyLoss,
+ * MSELoss, HuberLoss */
+enum vkc_loss { VKC_LOSS_CE = 0, VKC_LOSS_SCE = 1, VKC_LOSS_MSE = 2, VKC_LOSS_HUBER = 3 };
+
 typedef struct vkc_device* vkc_device_t;  /* one GPU + its streams        */
 typedef struct vkc_job* vkc_job_t;        /* completion marker (an event) */
 
@@ -95,7 +99,10 @@ int vkc_device_synchronize(vkc_device_t dev);
 /* The cudaStream_t all compute entry points use (as void*). */
 int vkc_device_stream(vkc_device_t dev, void** stream);
 /* Route subsequent work to `stream` (a cudaStream_t of the same device, e.g.
- * torch's current stream); NULL restores the device's own stream. */
+ * torch's current stream); NULL restores the device's own stream.  For the
+ * legacy default stream (handle 0 in most frameworks) pass cudaStreamLegacy
+ * ((void*)1): NULL would select the device's own non-blocking stream, which
+ * is not ordered with work on the default stream. */
 int vkc_device_set_stream(vkc_device_t dev, void* stream);
 /* Number of SMs and the device name (for logs and grid sizing). */
 int vkc_device_info(vkc_device_t dev, int* sm_count, char* name, size_t name_len);
@@ -117,6 +124,23 @@ int vkc_host_free(void* ptr);
  * the host only until the copy itself is done (not queued compute work).
  * Replaces GPU::toBuffer (_vkarray.cc:511-517, Buffer ctor 81-86). */
 int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void** dptr);
+/* vkc_upload without the host wait: returns once the copy is queued on the
+ * copy stream; the compute stream waits for it on the device, and `*job`
+ * completes with the copy.  `src` must be pinned (vkc_host_alloc) and stay
+ * unchanged until `*job` completes.  No reference counterpart (vulkpy's
+ * Buffer constructor copies synchronously, _vkarray.cc:81-86); lets the
+ * upload of the next batch overlap the current compute. */
+int vkc_upload_async(vkc_device_t dev, const void* src, size_t bytes, void** dptr, vkc_job_t* job);
+/* Device->host copy into pinned `dst` on a separate read-back stream, after
+ * every op issued so far on the compute stream but not after ops issued
+ * later, without a host wait; `*job` completes with the copy.  Lets the
+ * read-back of one batch's results overlap the next batch's compute.  Keep
+ * `src` allocated and `dst` untouched until `*job` completes.  No reference
+ * counterpart (vulkpy reads mapped memory, vkarray.py:186-188). */
+int vkc_d2h_async(vkc_device_t dev, void* dst, const void* src, size_t bytes, vkc_job_t* job);
+/* Make the compute stream wait (on the device) for `job`, e.g. before
+ * reusing memory that an asynchronous copy still reads. */
+int vkc_stream_wait_job(vkc_device_t dev, vkc_job_t job);
 /* Host->device copy into existing memory, ordered after queued compute work.
  * A pageable `src` is staged before the call returns.  A pinned `src` is
  * read when the stream reaches the copy: keep it unchanged until `*job`
@@ -146,6 +170,17 @@ int vkc_timer_record(vkc_device_t dev, vkc_job_t* job);
 int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms);
 /* Number of kernels this library has launched since load (all devices). */
 int vkc_launch_count(uint64_t* count);
+/* Number of device and pinned-host allocations this library has requested
+ * since load (vkc_alloc, vkc_upload, vkc_host_alloc and every scratch
+ * allocation inside an op).  No reference counterpart; lets a caller check
+ * that a call allocated nothing. */
+int vkc_alloc_count(uint64_t* count);
+/* Host-side fault injection for the allocation error path (the reference
+ * turns Vulkan allocation errors into RuntimeError, _vkarray.cc:32, 61-72):
+ * the allocation request `after` requests from now (0 = the next one) fails
+ * with VKC_ERR_OOM without calling CUDA; then injection switches itself
+ * off.  after < 0 switches it off.  Touches no GPU. */
+int vkc_inject_alloc_failure(int64_t after);
 
 /* ---- fused elementwise kernels (no reference counterpart: vulkpy runs one
  * shader per op).  `source` is CUDA C defining
@@ -218,10 +253,10 @@ int vkc_broadcast_to(vkc_device_t dev, const float* a, const int64_t* a_shape,
  * vkarray.py:1246-1274 (axis=None), sum.comp:18-30, sum_v1.3.comp:20-29. */
 int vkc_reduce_all(vkc_device_t dev, int op, int precision, const float* a, size_t n,
                    float* out, float scale);
-/* Same result contract as vkc_reduce_all, for callers that cannot allocate
- * device memory during the call (a host that hands the whole device heap to
- * its own allocator, or a latency-critical path where an allocation could
- * block or fail).  No counterpart in the reference.  The block partials
+/* The same launches and result as vkc_reduce_all, bit for bit, for callers
+ * that cannot allocate device memory during the call (a host that hands the
+ * whole device heap to its own allocator, or a latency-critical path where
+ * an allocation could block or fail).  No counterpart in the reference.  The block partials
  * live in a fixed 1 MiB device array inside the library, so n is limited to
  * 2^29 elements (larger n: VKC_ERR_INVALID).  The first call on a device
  * looks the array up (make it before capturing the stream); calls on one
@@ -389,12 +424,31 @@ int vkc_dense_backward(vkc_device_t dev, int precision, const float* x, const fl
 int vkc_dense_backward_act(vkc_device_t dev, int precision, const float* x, const float* w,
                            const float* dy_act, const float* y, int act, float* dy, float* dx,
                            float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim);
+/* vkc_dense_backward_act (act VKC_ACT_RELU / VKC_ACT_SIGMOID) or, with act
+ * VKC_ACT_NONE, vkc_dense_backward of dy_act (y and dy unused), with
+ * accumulate == 0 writing dW and db instead of adding to them: the values
+ * adding into zeroed gradients gives, without a zeroing pass.  The
+ * reference zeroes every gradient before each backward (Sequence.train,
+ * models.py:55-78, Parameter.zero_grad, parameters.py:81-86). */
+int vkc_dense_backward_ex(vkc_device_t dev, int precision, const float* x, const float* w,
+                          const float* dy_act, const float* y, int act, float* dy, float* dx,
+                          float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim,
+                          int accumulate);
 /* Row softmax over the last axis of [rows, cols] (nn/layers.py:297-300). */
 int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols);
 /* loss_rows[r] = sum_c -y log(p + 1e-8) with p = softmax(x) when softmax != 0
  * (else p = x); nn_cross_entropy.comp:21-26, losses.py:140-176, 218-249. */
 int vkc_cross_entropy(vkc_device_t dev, const float* x, const float* y, float* loss_rows,
                       float* p_out, int64_t rows, int64_t cols, int softmax);
+/* The softmax-cross-entropy loss step of one batch in two launches instead
+ * of three (losses.py:179-249 with ReduceLoss, losses.py:40-92): p_out =
+ * softmax(x) per row, dx = (p - y) * grad_scale, and *loss = (sum over rows
+ * of sum_c -y log(p + 1e-8)) * loss_scale, the rows added with the
+ * arithmetic of vkc_reduce_axis over a (rows,) vector, so the results equal
+ * vkc_cross_entropy + vkc_reduce_axis + vkc_softmax_ce_backward bit for bit.
+ * rows 1..2048. */
+int vkc_softmax_ce_fused(vkc_device_t dev, const float* x, const float* y, float* p_out, float* dx,
+                         float* loss, int64_t rows, int64_t cols, float loss_scale, float grad_scale);
 /* Adam step (optimizers.py:221-253) on n parameters, fused:
  * m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
  * value += -lr * (m / (1-b1t)) / (sqrt(v / (1-b2t)) + eps).  beta1t/beta2t
@@ -439,6 +493,48 @@ int vkc_cross_entropy_f64(vkc_device_t dev, const double* x, const double* y, do
                           double* p_out, int64_t rows, int64_t cols, int softmax);
 int vkc_softmax_ce_backward_f64(vkc_device_t dev, const double* p, const double* y, double* dx,
                                 size_t n, double scale);
+/* Per-row loss, loss_rows[r] = sum_c term(x[r,c], y[r,c]) over [rows, cols]:
+ * VKC_LOSS_CE -y log(x + 1e-8) (losses.py:95-176, nn_cross_entropy.comp:21-26);
+ * VKC_LOSS_SCE the same of p = softmax(x), p stored in p_out when not NULL
+ * (losses.py:179-249); VKC_LOSS_MSE (y - x)^2 (losses.py:252-320);
+ * VKC_LOSS_HUBER 0.5 min(|y - x|, (y - x)^2) (losses.py:323-393).  The
+ * batch reduction (ReduceLoss, losses.py:40-92) is the caller's. */
+int vkc_loss_rows(vkc_device_t dev, int kind, const float* x, const float* y, float* loss_rows,
+                  float* p_out, int64_t rows, int64_t cols);
+/* Gradient of a weighted sum of losses, one pass over n elements:
+ * dx = sum_j coeffs[j] * (grad_j * scales[j]), added in term order
+ * (MixLoss, losses.py:396-458; one term is a single loss).  grad_j:
+ * CE -y / (x + 1e-8) (nn_cross_entropy_backward.comp), SCE p - y
+ * (losses.py:229-249, p from vkc_loss_rows), MSE 2 (x - y), Huber
+ * clamp(x - y, -1, 1) as the reference (losses.py:376-393) or, with
+ * huber_exact != 0, the derivative of its forward (x - y where
+ * |x - y| <= 1, else 0.5 sign(x - y)).  scales[j] is the ReduceLoss
+ * factor (1/batch for a mean, losses.py:70-86).  nterms 1..8; the term
+ * tables are host memory.  float32 operations in the reference's order. */
+int vkc_loss_backward(vkc_device_t dev, int nterms, const int* kinds, const double* coeffs,
+                      const double* scales, int huber_exact, const float* x, const float* y,
+                      const float* p, float* dx, size_t n);
+/* Softmax backward with the full Jacobian: dx = y * (dy - sum_c dy y) per
+ * row of [rows, cols].  The reference's Softmax.backward keeps only the
+ * diagonal, dy y (1 - y) (layers.py:302-323; vkc_activation_backward with
+ * VKC_ACT_SIGMOID reproduces it). */
+int vkc_softmax_backward(vkc_device_t dev, const float* y, const float* dy, float* dx, int64_t rows,
+                         int64_t cols);
+/* Standalone ReLU max(x, 0) (layers.py:158-185) and Sigmoid
+ * 1 / (1 + exp(0 - x)) (layers.py:213-244, its four float32 array ops). */
+int vkc_activation_forward(vkc_device_t dev, int act, const float* x, float* y, size_t n);
+/* Float64 versions of the five entry points above, for finite-difference
+ * gradient checks; vkc_softmax_f64 is vkc_softmax in double.  No reference
+ * counterpart (vulkpy is float32 only). */
+int vkc_loss_rows_f64(vkc_device_t dev, int kind, const double* x, const double* y,
+                      double* loss_rows, double* p_out, int64_t rows, int64_t cols);
+int vkc_loss_backward_f64(vkc_device_t dev, int nterms, const int* kinds, const double* coeffs,
+                          const double* scales, int huber_exact, const double* x, const double* y,
+                          const double* p, double* dx, size_t n);
+int vkc_softmax_backward_f64(vkc_device_t dev, const double* y, const double* dy, double* dx,
+                             int64_t rows, int64_t cols);
+int vkc_activation_forward_f64(vkc_device_t dev, int act, const double* x, double* y, size_t n);
+int vkc_softmax_f64(vkc_device_t dev, const double* x, double* y, int64_t rows, int64_t cols);
 /* value += (-lr) * grad (optimizers.py:39-52). */
 int vkc_sgd_update(vkc_device_t dev, float* value, const float* grad, size_t n, double lr);
 /* h += g^2; value += (g / (sqrt(h) + eps)) * (-lr)  (optimizers.py:120-139). */

@@ -7,7 +7,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE_ROOT = os.environ.get("VULKPY_REFERENCE_ROOT", "/root/reference")
+# The reference source tree (vulkpy): $VULKPY_REFERENCE_ROOT, else a
+# directory named "reference" beside this repository.
+REFERENCE_ROOT = os.environ.get("VULKPY_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def pytest_configure(config):

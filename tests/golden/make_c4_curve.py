@@ -10,10 +10,12 @@ from integers(0, 10, 256); `steps` training steps.
 
 The reference's own Python (vulkpy/nn, vkarray.py, random.py) runs over the
 oracle's fake native module, about 12 s per step on 8 cores (its Dense
-backward materialises a 256 x 1024 x 1024 array), so the committed fixture
-has the first 200 steps (about 40 minutes).  Run where the reference source
+backward materialises a 256 x 1024 x 1024 array), so 1000 steps take a few
+hours; the file is rewritten every --save-every steps with the steps done
+so far (and the last layer's weights after them), so an interrupted run
+still leaves a consistent, shorter curve.  Run where the reference source
 tree exists:
-    python tests/golden/make_c4_curve.py [--steps 200] [--reference PATH]
+    python tests/golden/make_c4_curve.py [--steps 1000] [--reference PATH]
 """
 from __future__ import annotations
 
@@ -50,8 +52,9 @@ def build(vk):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("VULKPY_REFERENCE_ROOT", "/root/reference"))
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--reference", default=os.environ.get("VULKPY_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference")))
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--save-every", type=int, default=100)
     ap.add_argument("--out", default=os.path.join(HERE, "c4_loss_curve.npz"))
     args = ap.parse_args()
     from oracle.fake_vkarray import load_reference
@@ -59,14 +62,22 @@ def main():
     net, x, y = build(vk)
     losses = np.empty(args.steps, dtype=np.float32)
     t0 = time.time()
+
+    def save(done):
+        tmp = args.out + ".tmp.npz"
+        np.savez_compressed(tmp, loss=losses[:done], steps=np.array([done]),
+                            w_last=np.asarray(net.L[4].w.value).copy(), b_last=np.asarray(net.L[4].b.value).copy())
+        os.replace(tmp, args.out)
+        print(f"wrote {args.out} ({done} steps)", flush=True)
+
     for i in range(args.steps):
         _, loss = net.train(x, y)
         losses[i] = np.asarray(loss).reshape(-1)[0]
         if i % 50 == 0:
             print(f"step {i}: loss {losses[i]:.6f} ({time.time() - t0:.0f} s)", flush=True)
-    np.savez_compressed(args.out, loss=losses, steps=np.array([args.steps]),
-                        w_last=np.asarray(net.L[4].w.value).copy(), b_last=np.asarray(net.L[4].b.value).copy())
-    print(f"wrote {args.out}")
+        if (i + 1) % args.save_every == 0 and i + 1 < args.steps:
+            save(i + 1)
+    save(args.steps)
 
 
 if __name__ == "__main__":

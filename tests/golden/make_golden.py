@@ -32,7 +32,7 @@ def run_reference(reference_root: str) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("VULKPY_REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("VULKPY_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference")))
     ap.add_argument("--out", default=os.path.join(HERE, "golden.npz"))
     args = ap.parse_args()
     out = run_reference(args.reference)

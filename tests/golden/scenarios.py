@@ -381,6 +381,45 @@ def nn_train_steps(vk):
     return out
 
 
+def backward_suite_inputs():
+    """Seeded inputs of the layer / loss backward scenario (also used by the
+    autograd tests, which compare their Functions with its golden values):
+    logits and a gradient for the activations, probabilities and one-hot
+    labels for cross entropy, predictions and targets for MSE / Huber with
+    differences on both sides of the Huber kink (|d| = 1)."""
+    rng = np.random.default_rng(17)
+    z = rng.standard_normal((16, 7)).astype(np.float32) * np.float32(2)
+    dy = rng.standard_normal((16, 7)).astype(np.float32)
+    prob = rng.uniform(0.05, 1.0, (16, 7)).astype(np.float32)
+    prob /= prob.sum(axis=1, keepdims=True)
+    onehot = np.eye(7, dtype=np.float32)[rng.integers(0, 7, 16)]
+    pred = rng.standard_normal((16, 7)).astype(np.float32)
+    target = (pred + rng.standard_normal((16, 7)) * 1.5).astype(np.float32)
+    return z, dy, prob, onehot, pred, target
+
+
+@scenario(tol=("rtol", 2e-6, 1e-7))
+def nn_backward_suite(vk):
+    """Every layer's and loss's backward (and forward) on the seeded inputs
+    above: ReLU, Sigmoid, Softmax (the reference's diagonal form), cross
+    entropy, softmax cross entropy, MSE, Huber and a MixLoss of MSE and
+    Huber, each with the mean reduction's 1/batch scaling."""
+    g = vk.GPU()
+    nn = vk.nn
+    z, dy, prob, onehot, pred, target = backward_suite_inputs()
+    out = {}
+    for name, layer in (("relu", nn.ReLU()), ("sigmoid", nn.Sigmoid()), ("softmax", nn.Softmax())):
+        out[f"{name}_y"] = A(layer(vk.Array(g, data=z)))
+        out[f"{name}_dx"] = A(layer.backward(vk.Array(g, data=dy)))
+    cases = (("ce", nn.CrossEntropyLoss(), prob, onehot), ("sce", nn.SoftmaxCrossEntropyLoss(), z, onehot),
+             ("mse", nn.MSELoss(), pred, target), ("huber", nn.HuberLoss(), pred, target),
+             ("mix", nn.losses.MixLoss([(0.3, nn.MSELoss()), (0.7, nn.HuberLoss())]), pred, target))
+    for name, loss, x, y in cases:
+        out[f"{name}_loss"] = A(loss(vk.Array(g, data=x), vk.Array(g, data=y)))
+        out[f"{name}_dx"] = A(loss.grad())
+    return out
+
+
 # ------------------------------------------------------------ small op suite
 def _suite_inputs():
     rng = np.random.default_rng(0)

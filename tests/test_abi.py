@@ -80,3 +80,23 @@ def test_grouped_entry_points_validate_without_gpu():
     assert L.vkc_sgd_update_grouped(None, ptrs, ptrs, n, 1e-2, 1) == _lib.ERR_INVALID
     s, t = C.c_int(), C.c_int()
     assert L.vkc_gemm_plan_get(None, _lib.MM_BF16X3, 256, 1024, 784, C.byref(s), C.byref(t)) == _lib.ERR_INVALID
+
+
+def test_injected_host_allocation_failure_without_gpu():
+    """The allocation error path is testable on the host: an injected failure
+    returns VKC_ERR_OOM before any CUDA call, counts as an allocation
+    request, and switches itself off after firing."""
+    import ctypes as C
+    from vulkpy_gb300 import _lib
+    L = _lib.lib
+    c0, c1 = C.c_uint64(), C.c_uint64()
+    assert L.vkc_alloc_count(C.byref(c0)) == _lib.OK
+    p = C.c_void_p()
+    try:
+        assert L.vkc_inject_alloc_failure(0) == _lib.OK
+        assert L.vkc_host_alloc(4096, C.byref(p)) == _lib.ERR_OOM and not p.value
+        assert "injected allocation failure" in _lib.last_error()
+    finally:
+        L.vkc_inject_alloc_failure(-1)
+    assert L.vkc_alloc_count(C.byref(c1)) == _lib.OK and c1.value == c0.value + 1
+    assert L.vkc_alloc_count(None) == _lib.ERR_INVALID

@@ -156,3 +156,125 @@ def test_graph_output_tracked_when_python_reuses_ids(gpu, vk):
         x[:] = base * (k + 1)
         g.launch(flush=[x])
         np.testing.assert_array_equal(np.asarray(out), base * (k + 1) + 1.0, err_msg=f"launch {k}, reused={reused}")
+
+
+def test_enable_debug_raises_at_the_failing_op(gpu, vk):
+    """util.enable_debug (vulkpy/util.py:19-54 turns on Vulkan validation
+    layers): here every op synchronises and reads the device error word, so
+    an out-of-range gather raises at that op rather than silently writing
+    NaN; the ops before and after it run normally."""
+    a = vk.Array(gpu, data=np.arange(10, dtype=np.float32))
+    good = vk.U32Array(gpu, data=[1, 2, 3])
+    bad = vk.U32Array(gpu, data=[1, 10, 3])
+    gpu.check_errors()
+    vk.util.enable_debug(api_dump=False)
+    try:
+        assert vk.util.debug_enabled()
+        np.testing.assert_array_equal(np.asarray(a.gather(good)), [1, 2, 3])
+        with pytest.raises(IndexError, match="gather index out of range"):
+            a.gather(bad)
+        np.testing.assert_array_equal(np.asarray(a + 1.0)[:2], [1, 2])
+    finally:
+        vk.util.disable_debug()
+    assert not vk.util.debug_enabled()
+    out = a.gather(bad)              # without debug: NaN and the flag, no exception
+    assert np.isnan(np.asarray(out)[1])
+    assert gpu.check_errors() & 1
+
+
+def test_injected_allocation_failures_raise_and_recover(gpu, vk):
+    """Allocation failures injected on the host (vkc_inject_alloc_failure,
+    no GPU fault): an array allocation, an upload, a pinned host buffer and
+    an op's internal scratch each fail with MemoryError at the call that
+    allocates, and the device keeps working afterwards."""
+    from vulkpy_gb300 import _lib
+    lib = _lib.lib
+    x = vk.Array(gpu, data=np.ones((256, 256), dtype=np.float32))
+    try:
+        assert lib.vkc_inject_alloc_failure(0) == 0
+        with pytest.raises(MemoryError, match="injected allocation failure"):
+            vk.Array(gpu, shape=(1000,))
+        assert lib.vkc_inject_alloc_failure(0) == 0
+        with pytest.raises(MemoryError, match="injected allocation failure"):
+            vk.Array(gpu, data=np.ones(1000, dtype=np.float32))
+        p = C.c_void_p()
+        assert lib.vkc_inject_alloc_failure(0) == 0
+        assert lib.vkc_host_alloc(1 << 20, C.byref(p)) == _lib.ERR_OOM and not p.value
+        assert "injected" in _lib.last_error()
+        # the second allocation of a bf16 matmul is its operand scratch (the
+        # first is the result array)
+        assert lib.vkc_inject_alloc_failure(1) == 0
+        with pytest.raises(MemoryError, match="injected allocation failure"):
+            vk.vkarray.matmul(x, x, precision="bf16")
+    finally:
+        lib.vkc_inject_alloc_failure(-1)
+    c = vk.vkarray.matmul(x, x, precision="bf16")
+    np.testing.assert_allclose(np.asarray(c), np.full((256, 256), 256.0), rtol=1e-6)
+    assert gpu.check_errors() == 0
+
+
+def test_async_pinned_upload_and_prefetch(gpu, vk):
+    """Array(data=pinned) returns once the copy is queued; ops on the array
+    wait for it on the device.  prefetch() starts the read-back without
+    waiting; a read after it returns the values of the ops issued before it,
+    and a write after it makes the prefetched copy stale (not used)."""
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((1024, 1024)).astype(np.float32)
+    xp = vk.vkarray.empty_pinned(x.shape)
+    xp[...] = x
+    a = vk.Array(gpu, data=xp)
+    b = a * 2.0
+    a.wait()                       # the upload is done: the source may change
+    xp[...] = 0.0
+    np.testing.assert_array_equal(np.asarray(b), x * 2.0)
+    np.testing.assert_array_equal(np.asarray(a), x)
+    c = a + 1.0
+    c.prefetch()
+    d = c * 3.0                    # issued after the prefetch, reads c
+    np.testing.assert_array_equal(np.asarray(c), x + 1.0)
+    np.testing.assert_array_equal(np.asarray(d), (x + 1.0) * 3.0)
+    c.prefetch()                   # already on the host: nothing to do
+    e = a - 1.0
+    e.prefetch()
+    e += 10.0                      # written after the prefetch
+    np.testing.assert_array_equal(np.asarray(e), (x - 1.0) + 10.0)
+    f = a * 0.5
+    f.prefetch()
+    del f                          # dropped with its read-back in flight
+    gpu.wait()
+
+
+def test_pipelined_steps_match_serial(gpu, vk):
+    """The pipelined loop of the end-to-end benchmark (issue step i+1 before
+    reading step i's prefetched results) gives the serial loop's values."""
+    rng = np.random.default_rng(6)
+    hs = [rng.standard_normal((512, 2048)).astype(np.float32) for _ in range(4)]
+    row = rng.uniform(0.5, 2, (1, 2048)).astype(np.float32)
+    r = vk.Array(gpu, data=row)
+
+    def step(h):
+        X = vk.Array(gpu, data=h)
+        X *= r
+        s = X.sum(axis=1)
+        m = X.maximum(axis=0)
+        return [s, m, X]
+
+    serial = [[np.asarray(o).copy() for o in step(h)] for h in hs]
+    pins = []
+    for h in hs:
+        p = vk.vkarray.empty_pinned(h.shape)
+        p[...] = h
+        pins.append(p)
+    got, pending = [], None
+    for p in pins + [None]:
+        cur = None
+        if p is not None:
+            cur = step(p)
+            for o in cur:
+                o.prefetch()
+        if pending is not None:
+            got.append([np.asarray(o).copy() for o in pending])
+        pending = cur
+    for a, b in zip(serial, got):
+        for u, v in zip(a, b):
+            np.testing.assert_array_equal(u, v)

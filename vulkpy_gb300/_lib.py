@@ -33,6 +33,7 @@ ARGMAX, ARGMIN = range(2)
 RED_PLAIN, RED_PAIRWISE, RED_COMPENSATED = range(3)
 MM_FP32, MM_BF16, MM_BF16X3 = range(3)
 ACT_NONE, ACT_RELU, ACT_SIGMOID = range(3)
+LOSS_CE, LOSS_SCE, LOSS_MSE, LOSS_HUBER = range(4)
 
 vp = C.c_void_p
 sz = C.c_size_t
@@ -70,6 +71,9 @@ _SIGS = {
     "vkc_host_free": ([vp], i32),
     "vkc_upload": ([vp, vp, sz, C.POINTER(vp)], i32),
     "vkc_h2d": ([vp, vp, vp, sz, C.POINTER(vp)], i32),
+    "vkc_upload_async": ([vp, vp, sz, C.POINTER(vp), C.POINTER(vp)], i32),
+    "vkc_d2h_async": ([vp, vp, vp, sz, C.POINTER(vp)], i32),
+    "vkc_stream_wait_job": ([vp, vp], i32),
     "vkc_d2h": ([vp, vp, vp, sz], i32),
     "vkc_fill_f32": ([vp, vp, sz, f32], i32),
     "vkc_fill_u32": ([vp, vp, sz, u32], i32),
@@ -81,6 +85,8 @@ _SIGS = {
     "vkc_timer_record": ([vp, C.POINTER(vp)], i32),
     "vkc_job_elapsed_ms": ([vp, vp, C.POINTER(C.c_float)], i32),
     "vkc_launch_count": ([C.POINTER(C.c_uint64)], i32),
+    "vkc_alloc_count": ([C.POINTER(C.c_uint64)], i32),
+    "vkc_inject_alloc_failure": ([i64], i32),
     "vkc_binary": ([vp, i32, vp, vp, vp, sz], i32),
     "vkc_binary_scalar": ([vp, i32, vp, f32, vp, sz], i32),
     "vkc_unary": ([vp, i32, vp, vp, sz], i32),
@@ -118,6 +124,7 @@ _SIGS = {
     "vkc_dense_forward": ([vp, i32, vp, vp, vp, vp, i64, i64, i64, i32], i32),
     "vkc_dense_backward": ([vp, i32, vp, vp, vp, vp, vp, vp, i64, i64, i64], i32),
     "vkc_dense_backward_act": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64], i32),
+    "vkc_dense_backward_ex": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64, i32], i32),
     "vkc_softmax": ([vp, vp, vp, i64, i64], i32),
     "vkc_cross_entropy": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
     "vkc_adam_update": ([vp, vp, vp, vp, vp, sz, f64, f64, f64, f64, f64, f64], i32),
@@ -130,6 +137,7 @@ _SIGS = {
     "vkc_cross_entropy_f64": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
     "vkc_softmax_ce_backward_f64": ([vp, vp, vp, vp, sz, f64], i32),
     "vkc_softmax_ce_backward": ([vp, vp, vp, vp, sz, f32], i32),
+    "vkc_softmax_ce_fused": ([vp, vp, vp, vp, vp, vp, i64, i64, f32, f32], i32),
     "vkc_jit_compile": ([vp, C.c_char_p, C.c_char_p, C.POINTER(vp)], i32),
     "vkc_jit_launch": ([vp, vp, C.POINTER(vp), i32, C.POINTER(vp), i32, sz], i32),
     "vkc_stream_create": ([vp, C.POINTER(vp)], i32),
@@ -140,6 +148,17 @@ _SIGS = {
     "vkc_graph_launch": ([vp], i32),
     "vkc_graph_destroy": ([vp], i32),
     "vkc_adagrad_update": ([vp, vp, vp, vp, sz, f64, f64], i32),
+    "vkc_loss_rows": ([vp, i32, vp, vp, vp, vp, i64, i64], i32),
+    "vkc_loss_rows_f64": ([vp, i32, vp, vp, vp, vp, i64, i64], i32),
+    "vkc_loss_backward": ([vp, i32, C.POINTER(C.c_int), C.POINTER(f64), C.POINTER(f64), i32, vp, vp, vp, vp, sz],
+                          i32),
+    "vkc_loss_backward_f64": ([vp, i32, C.POINTER(C.c_int), C.POINTER(f64), C.POINTER(f64), i32, vp, vp, vp, vp,
+                               sz], i32),
+    "vkc_softmax_backward": ([vp, vp, vp, vp, i64, i64], i32),
+    "vkc_softmax_backward_f64": ([vp, vp, vp, vp, i64, i64], i32),
+    "vkc_activation_forward": ([vp, i32, vp, vp, sz], i32),
+    "vkc_activation_forward_f64": ([vp, i32, vp, vp, sz], i32),
+    "vkc_softmax_f64": ([vp, vp, vp, i64, i64], i32),
 }
 
 for _name, (_args, _res) in _SIGS.items():

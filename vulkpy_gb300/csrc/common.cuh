@@ -22,6 +22,8 @@ struct vkc_device {
   cudaStream_t stream = nullptr;       // current compute stream (own or user's)
   cudaStream_t copy_stream = nullptr;  // uploads into fresh buffers
   cudaEvent_t copy_done = nullptr;     // reused marker for uploads
+  cudaStream_t d2h_stream = nullptr;   // asynchronous read-backs (vkc_d2h_async)
+  cudaEvent_t d2h_after = nullptr;     // reused marker: compute work a read-back follows
   cudaStream_t side_stream = nullptr;  // independent work forked from `stream` inside one call
   cudaEvent_t side_fork = nullptr, side_join = nullptr;
   uint32_t* err_word = nullptr;        // device error flags (bit0: gather index)
@@ -46,6 +48,10 @@ void clear_error();
 int bind(vkc_device_t dev);
 
 extern std::atomic<uint64_t> g_launches;  // kernels launched (all devices)
+
+// Counts an allocation request and reports whether an injected failure
+// (vkc_inject_alloc_failure) falls on it.
+bool alloc_should_fail();
 
 inline int check_launch(const char* what) {
   g_launches.fetch_add(1, std::memory_order_relaxed);

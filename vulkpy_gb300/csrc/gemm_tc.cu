@@ -329,34 +329,21 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& h, __nv_bfloa
   l = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
-// K contiguous in the source: dst[r*Kp + k] from src[r*ld + k]; zero padding k >= K.
-__global__ void k_split_kmajor(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
-                               __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
-  const int64_t total = R * Kp;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-    const int64_t r = i / Kp, k = i - r * Kp;
-    const float x = k < K ? src[r * ld + k] : 0.f;
-    __nv_bfloat16 h, l;
-    split_bf16(x, h, l);
-    hi[i] = h;
-    if (lo) lo[i] = l;
-  }
-}
-
-// The same with 8 elements per thread: 2 x float4 in, one 16-byte store per
-// output (ld % 4 == 0, 16-byte aligned source, Kp % 8 == 0); the chunk that
-// straddles K is read element by element, chunks past K are zero.  Blocks
-// `blk` of `nblk` stride over the chunks.
+// K contiguous in the source: dst[r*Kp + k] from src[r*ld + k], zero padding
+// k >= K.  8 elements per thread: 2 x float4 in (`vec`: ld % 4 == 0 and a
+// 16-byte aligned source; otherwise element loads), one 16-byte store per
+// output (Kp % 8 == 0); the chunk that straddles K is read element by
+// element, chunks past K are zero.  Blocks `blk` of `nblk` stride over the
+// chunks.
 __device__ __forceinline__ void split_kmajor8_body(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
                                                    __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                                                   int64_t Kp, int64_t blk, int64_t nblk) {
+                                                   int64_t Kp, int64_t blk, int64_t nblk, bool vec = true) {
   const int64_t per_row = Kp / 8, total = R * per_row;
   const int64_t stride = nblk * blockDim.x;
   for (int64_t i = blk * blockDim.x + threadIdx.x; i < total; i += stride) {
     const int64_t r = i / per_row, k = (i - r * per_row) * 8;
     float x[8];
-    if (k + 8 <= K) {
+    if (vec && k + 8 <= K) {
       const float4* p = reinterpret_cast<const float4*>(src + r * ld + k);
       const float4 v0 = *p, v1 = *(p + 1);
       x[0] = v0.x, x[1] = v0.y, x[2] = v0.z, x[3] = v0.w, x[4] = v1.x, x[5] = v1.y, x[6] = v1.z, x[7] = v1.w;
@@ -372,22 +359,18 @@ __device__ __forceinline__ void split_kmajor8_body(const float* __restrict__ src
   }
 }
 
-__global__ void __launch_bounds__(256)
-k_split_kmajor8(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
-                __nv_bfloat16* __restrict__ lo, int64_t Kp) {
-  split_kmajor8_body(src, R, K, ld, hi, lo, Kp, blockIdx.x, gridDim.x);
-}
-
 // K is the row index of the source (src[k*ld + r]): 64 (k) x 64 (r) tiles
 // through shared memory.  Reads: each thread one float4 of a k row (16 rows
-// of 256 bytes per pass); writes: each thread 8 consecutive k of one r as a
-// 16-byte store (8 rows of 128 bytes per pass).  Requires ld % 4 == 0 and a
-// 16-byte aligned source; R need not be a multiple of 4 (the tail of a
-// row is read element by element).  256 threads; tile (bx, by) covers rows
-// r in [64 bx, 64 bx + 64), k in [64 by, 64 by + 64).
+// of 256 bytes per pass; with `vec` false -- ld % 4 != 0 or an unaligned
+// source -- four element loads); writes: each thread 8 consecutive k of one
+// r as a 16-byte store (8 rows of 128 bytes per pass).  R need not be a
+// multiple of 4 (the tail of a row is read element by element).  256
+// threads; tile (bx, by) covers rows r in [64 bx, 64 bx + 64), k in
+// [64 by, 64 by + 64).
 __device__ __forceinline__ void split_transpose_body(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
                                                      __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                                                     int64_t Kp, int64_t bx, int64_t by, float (*tile)[65]) {
+                                                     int64_t Kp, int64_t bx, int64_t by, float (*tile)[65],
+                                                     bool vec = true) {
   const int64_t r0 = bx * 64, k0 = by * 64;
   const int t = threadIdx.x;
   {
@@ -398,8 +381,10 @@ __device__ __forceinline__ void split_transpose_body(const float* __restrict__ s
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (k < K) {
         const float* p = src + k * ld + r;
-        if (r + 3 < R) {
+        if (vec && r + 3 < R) {
           v = *reinterpret_cast<const float4*>(p);
+        } else if (r + 3 < R) {
+          v = make_float4(p[0], p[1], p[2], p[3]);
         } else {
           if (r < R) v.x = p[0];
           if (r + 1 < R) v.y = p[1];
@@ -427,13 +412,6 @@ __device__ __forceinline__ void split_transpose_body(const float* __restrict__ s
   }
 }
 
-__global__ void __launch_bounds__(256)
-k_split_transpose(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld, __nv_bfloat16* __restrict__ hi,
-                  __nv_bfloat16* __restrict__ lo, int64_t Kp) {
-  __shared__ float tile[64][65];
-  split_transpose_body(src, R, K, ld, hi, lo, Kp, blockIdx.x, blockIdx.y, tile);
-}
-
 // Both operands of a GEMM in one launch (two launches cost more than the
 // conversion itself for the small GEMMs of an MLP step): blocks [0, a.blocks)
 // convert op(A), the rest op(B).
@@ -444,6 +422,7 @@ struct SplitJob {
   __nv_bfloat16* lo;
   int64_t tiles_x;  // transpose: tiles along R; 0: K contiguous (8 per thread)
   int64_t blocks;
+  int vec;          // 16-byte loads allowed (ld % 4 == 0, aligned source)
 };
 
 __global__ void __launch_bounds__(256) k_split_pair(const __grid_constant__ SplitJob a,
@@ -453,71 +432,20 @@ __global__ void __launch_bounds__(256) k_split_pair(const __grid_constant__ Spli
   const SplitJob& j = first ? a : b;
   const int64_t blk = first ? (int64_t)blockIdx.x : (int64_t)blockIdx.x - a.blocks;
   if (j.tiles_x == 0)
-    split_kmajor8_body(j.src, j.R, j.K, j.ld, j.hi, j.lo, j.Kp, blk, j.blocks);
+    split_kmajor8_body(j.src, j.R, j.K, j.ld, j.hi, j.lo, j.Kp, blk, j.blocks, j.vec != 0);
   else
-    split_transpose_body(j.src, j.R, j.K, j.ld, j.hi, j.lo, j.Kp, blk % j.tiles_x, blk / j.tiles_x, tile);
+    split_transpose_body(j.src, j.R, j.K, j.ld, j.hi, j.lo, j.Kp, blk % j.tiles_x, blk / j.tiles_x, tile, j.vec != 0);
 }
 
-// Fallback for unaligned sources: 32 x 32 tiles, one element per access.
-__global__ void k_split_transpose1(const float* __restrict__ src, int64_t R, int64_t K, int64_t ld,
-                                   __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t Kp) {
-  __shared__ float tile[32][33];
-  const int64_t r0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
-  for (int j = ty; j < 32; j += 8) {
-    const int64_t k = k0 + j, r = r0 + tx;
-    tile[j][tx] = (k < K && r < R) ? src[k * ld + r] : 0.f;
-  }
-  __syncthreads();
-  for (int j = ty; j < 32; j += 8) {
-    const int64_t r = r0 + j, k = k0 + tx;
-    if (r < R && k < Kp) {
-      __nv_bfloat16 h, l;
-      split_bf16(tile[tx][j], h, l);
-      hi[r * Kp + k] = h;
-      if (lo) lo[r * Kp + k] = l;
-    }
-  }
-}
-
-// Produce K-major bf16 copies of a logical (R x K) operand.  `k_contig`:
-// element (r, k) is src[r*ld + k]; otherwise src[k*ld + r].
-int split_operand(vkc_device_t dev, const float* src, int64_t R, int64_t K, int64_t ld, bool k_contig,
-                  __nv_bfloat16* hi, __nv_bfloat16* lo, int64_t Kp) {
-  if (k_contig) {
-    if (ld % 4 == 0 && ((uintptr_t)src & 15u) == 0) {
-      unsigned grid = wave_grid(dev, k_split_kmajor8, (size_t)(R * (Kp / 8)), 256);
-      k_split_kmajor8<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
-    } else {
-      unsigned grid = stream_grid(dev, (size_t)(R * Kp), 256);
-      k_split_kmajor<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
-    }
-  } else if (ld % 4 == 0 && ((uintptr_t)src & 15u) == 0) {
-    dim3 grid((unsigned)((R + 63) / 64), (unsigned)((Kp + 63) / 64));
-    if (grid.y > 65535) return set_error(VKC_ERR_INVALID, "matmul: K too large for the transpose pre-pass");
-    k_split_transpose<<<grid, 256, 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
-  } else {
-    dim3 grid((unsigned)((R + 31) / 32), (unsigned)((Kp + 31) / 32));
-    if (grid.y > 65535) return set_error(VKC_ERR_INVALID, "matmul: K too large for the transpose pre-pass");
-    k_split_transpose1<<<grid, dim3(32, 8), 0, dev->stream>>>(src, R, K, ld, hi, lo, Kp);
-  }
-  return check_launch("split_operand");
-}
-
-// Both operands: one k_split_pair launch when both sources allow the vector
-// paths, else one launch each.
+// Both operands in one k_split_pair launch (16-byte loads where a source
+// allows them, element loads where it does not).
 int split_operands(vkc_device_t dev, const float* A, int64_t M, int64_t lda, bool a_kcontig, __nv_bfloat16* a_hi,
                    __nv_bfloat16* a_lo, const float* B, int64_t N, int64_t ldb, bool b_kcontig,
                    __nv_bfloat16* b_hi, __nv_bfloat16* b_lo, int64_t K, int64_t Kp) {
   auto aligned = [](const float* p, int64_t ld) { return ld % 4 == 0 && ((uintptr_t)p & 15u) == 0; };
-  if (!aligned(A, lda) || !aligned(B, ldb) || (Kp + 63) / 64 > 65535) {
-    int r = split_operand(dev, A, M, K, lda, a_kcontig, a_hi, a_lo, Kp);
-    if (r == VKC_OK) r = split_operand(dev, B, N, K, ldb, b_kcontig, b_hi, b_lo, Kp);
-    return r;
-  }
   const int64_t cap = (int64_t)dev->sm_count * resident_blocks((const void*)k_split_pair, 256);
   auto job = [&](const float* src, int64_t R, int64_t ld, bool kcontig, __nv_bfloat16* hi, __nv_bfloat16* lo) {
-    SplitJob j{src, R, K, ld, Kp, hi, lo, 0, 0};
+    SplitJob j{src, R, K, ld, Kp, hi, lo, 0, 0, aligned(src, ld) ? 1 : 0};
     if (kcontig) {
       j.blocks = std::max<int64_t>(1, std::min<int64_t>((R * (Kp / 8) + 255) / 256, cap));
     } else {

@@ -173,19 +173,35 @@ __global__ void __launch_bounds__(256) k_tile_operands(const __grid_constant__ T
 }
 
 // ------------------------------------------------------------ tensor cores
+// One problem as the kernel walks it.  A problem with M <= 64 < N runs
+// swapped (C^T = op(B)^T op(A)^T): its small dimension becomes the MMA's N,
+// so a tile multiplies 128 x roundup16(M) instead of padding M to 128 rows.
+// The kernel's tile grid is mk x nk (mk = M, nk = N, or the reverse when
+// swapped); a tile's MMA is 128 x bn with bn the columns left, rounded up to
+// 16 (at most 128), and the last K block issues only the 16-wide K steps
+// that hold data (the operand tiles are zero past K, so the skipped steps
+// would add exact zeros).
 struct TcProb {
-  const uint8_t* a_hi;  // tiles of op(A): [M/128][K/64] x 16 KB
+  const uint8_t* a_hi;  // tiles of the kernel's A side: [mk/128][K/64] x 16 KB
   const uint8_t* a_lo;
-  const uint8_t* b_hi;  // tiles of op(B)^T: [N/128][K/64] x 16 KB
+  const uint8_t* b_hi;  // tiles of the kernel's B side: [nk/128][K/64] x 16 KB
   const uint8_t* b_lo;
   float* c;
   const float* bias;
   const float* mask;
   int64_t ldc;
-  int m, n, kt;  // kt: 64-wide K blocks (>= 1)
+  int m, n, kt;  // m x n: C's shape; kt: 64-wide K blocks (>= 1)
+  int nk;        // columns of the kernel's tile grid (n, or m when swapped)
+  int klast;     // 16-wide K steps in the last K block (1..4)
+  int swap;
   float alpha, beta;
   int act, tiles_n, tile0;
 };
+
+__device__ __forceinline__ int tile_bn(const TcProb& P, int n0) {
+  const int left = P.nk - n0;
+  return left >= 128 ? 128 : ((left + 15) & ~15);
+}
 
 struct TcTable {
   int count, total;
@@ -265,18 +281,21 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
     for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
       const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
       const int local = t - P.tile0;
+      const int tn = local % P.tiles_n;
       const size_t a_off = (size_t)(local / P.tiles_n) * P.kt * kTileBytes;
-      const size_t b_off = (size_t)(local % P.tiles_n) * P.kt * kTileBytes;
+      const size_t b_off = (size_t)tn * P.kt * kTileBytes;
+      // only the B tile's first bn rows (bn * 128 contiguous bytes) are used
+      const uint32_t b_bytes = (uint32_t)tile_bn(P, tn * BN) * 128u;
       for (int kb = 0; kb < P.kt; ++kb, ++g) {
         const int s = g % S;
         if (*abort_flag || !mbar_wait(empty_bar(s), ((g / S) & 1) ^ 1)) { ok = false; break; }
-        mbar_expect_tx(full_bar(s), Cfg::kStageBytes);
+        mbar_expect_tx(full_bar(s), (X3 ? 2u : 1u) * (kTileBytes + b_bytes));
         const size_t kofs = (size_t)kb * kTileBytes;
         bulk_load(stage(s, 0), P.a_hi + a_off + kofs, kTileBytes, full_bar(s));
-        bulk_load(stage(s, 1), P.b_hi + b_off + kofs, kTileBytes, full_bar(s));
+        bulk_load(stage(s, 1), P.b_hi + b_off + kofs, b_bytes, full_bar(s));
         if (X3) {
           bulk_load(stage(s, 2), P.a_lo + a_off + kofs, kTileBytes, full_bar(s));
-          bulk_load(stage(s, 3), P.b_lo + b_off + kofs, kTileBytes, full_bar(s));
+          bulk_load(stage(s, 3), P.b_lo + b_off + kofs, b_bytes, full_bar(s));
         }
       }
     }
@@ -289,12 +308,13 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
-    constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                               ((uint32_t)(kTileRows >> 4) << 24);
     uint32_t g = 0, acc = 0;  // g: K blocks (stage ring), acc: accumulations (TMEM ring)
     bool ok = true;
     for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
       const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
+      const int bn = tile_bn(P, ((t - P.tile0) % P.tiles_n) * BN);
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(bn >> 3) << 17) |
+                             ((uint32_t)(kTileRows >> 4) << 24);
       const int span = X3 ? kDrainX3 : P.kt;  // K blocks per TMEM accumulation
       for (int g0 = 0; g0 < P.kt && ok; g0 += span, ++acc) {
         const int b = acc % kAccBufs;
@@ -306,15 +326,25 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
           const int s = g % S;
           if (*abort_flag || !mbar_wait(full_bar(s), (g / S) & 1)) { ok = false; break; }
           tc_fence_after();
+          const int ksteps = kb == P.kt - 1 ? P.klast : kTileK / 16;
 #pragma unroll
           for (int k = 0; k < kTileK / 16; ++k) {
+            if (k >= ksteps) break;
             const uint64_t a = sw128_desc(stage(s, 0) + 32u * k);
             const uint64_t bb = sw128_desc(stage(s, 1) + 32u * k);
             const uint32_t first = (kb == g0 && k == 0) ? 0u : 1u;
             if (X3) {
-              // the same order as k_gemm_tcp: cross terms, then hi*hi
-              mma_bf16(d, a, sw128_desc(stage(s, 3) + 32u * k), idesc, first);
-              mma_bf16(d, sw128_desc(stage(s, 2) + 32u * k), bb, idesc, 1);
+              // the same order of products as k_gemm_tcp: op(A)_hi op(B)_lo,
+              // op(A)_lo op(B)_hi, then hi*hi (a swapped problem has op(B)
+              // on the A side, so its cross terms come in the other order)
+              const uint64_t alo = sw128_desc(stage(s, 2) + 32u * k), blo = sw128_desc(stage(s, 3) + 32u * k);
+              if (P.swap) {
+                mma_bf16(d, alo, bb, idesc, first);
+                mma_bf16(d, a, blo, idesc, 1);
+              } else {
+                mma_bf16(d, a, blo, idesc, first);
+                mma_bf16(d, alo, bb, idesc, 1);
+              }
               mma_bf16(d, a, bb, idesc, 1);
             } else {
               mma_bf16(d, a, bb, idesc, first);
@@ -345,6 +375,7 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
     for (int t = blockIdx.x; t < tab.total && ok; t += gridDim.x) {
       const TcProb& P = tab.p[find_problem(tab.p, tab.count, t)];
       const int local = t - P.tile0;
+      // kernel coordinates: rows m0 (TMEM lanes), columns n0 (TMEM columns)
       const int m0 = (local / P.tiles_n) * kTileRows, n0 = (local % P.tiles_n) * BN + hc * CW;
       const int span = X3 ? kDrainX3 : P.kt;
       const int ngroups = (P.kt + span - 1) / span;
@@ -391,12 +422,18 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
       float* stage = reinterpret_cast<float*>(gbase + Cfg::kEpiOff) + (warp - 2) * (kEpiStageBytes / 4);
 #pragma unroll 1
       for (int c = 0; c < CW / 32; ++c) {  // one copy of the epilogue code
+        const int col0 = n0 + c * 32;
+        if (col0 >= P.nk) break;
         uint32_t r[32];
         tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + c * 32), r);
-        const int col0 = n0 + c * 32;
-        if (m0 + q * 32 < P.m && col0 < P.n)
+        if (P.swap) {
+          // lanes are columns of C (kernel rows), TMEM columns rows of C
+          if (m0 + q * 32 < P.n)
+            epilogue_tile32_t(r, P.c, P.mask, P.bias, P.ldc, m0 + q * 32, P.n, col0, P.m, P.alpha, P.beta, P.act);
+        } else if (m0 + q * 32 < P.m) {
           epilogue_tile32(r, stage, P.c, P.mask, P.bias, P.ldc, m0 + q * 32, P.m, col0, P.n, P.alpha, P.beta, P.act,
                           false);
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -790,10 +827,14 @@ int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const s
       ttotal += nt * kt;
 
       TcProb& P = tab.p[tab.count++];
-      P.a_hi = a_hi;
-      P.a_lo = a_lo;
-      P.b_hi = b_hi;
-      P.b_lo = b_lo;
+      const bool swap = q.m <= 64 && q.n > 64;
+      P.swap = swap ? 1 : 0;
+      P.a_hi = swap ? b_hi : a_hi;
+      P.a_lo = swap ? b_lo : a_lo;
+      P.b_hi = swap ? a_hi : b_hi;
+      P.b_lo = swap ? a_lo : b_lo;
+      P.nk = (int)(swap ? q.m : q.n);
+      P.klast = (int)(((q.k - (int64_t)(kt - 1) * kTileK) + 15) / 16);
       P.c = q.c;
       P.bias = q.bias;
       P.mask = q.relu_mask;
@@ -804,7 +845,7 @@ int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const s
       P.alpha = q.alpha;
       P.beta = q.beta;
       P.act = q.act;
-      P.tiles_n = nt;
+      P.tiles_n = swap ? mt : nt;
       P.tile0 = total;
       total += mt * nt;
     }

@@ -15,6 +15,7 @@
 #include "gemm_simt.cuh"
 #include "gemm_tc.cuh"
 #include "colsum.cuh"
+#include "reduce_acc.cuh"
 
 namespace {
 
@@ -34,13 +35,16 @@ int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64
   return vkc::set_error(VKC_ERR_INVALID, "unknown matmul precision %d", precision);
 }
 
-// db[o] += sum_b dy[b, o], b in order (one block per 32 columns).
-__global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db) {
+// db[o] += sum_b dy[b, o], b in order (one block per 32 columns);
+// `overwrite`: db[o] = the sum, the value adding it to a zeroed gradient
+// gives (the sum starts at +0, so it is never -0).
+__global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db,
+                                                    int overwrite) {
   __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
   const int64_t c0 = (int64_t)blockIdx.x * vkc::kColsumCols;
   const float s = vkc::colsum32(dy, batch, out_dim, out_dim, c0, tile);
   const int64_t o = c0 + threadIdx.x;
-  if (threadIdx.x < 32 && o < out_dim) db[o] += s;
+  if (threadIdx.x < 32 && o < out_dim) db[o] = overwrite ? s : db[o] + s;
 }
 
 // db[o] += sum_b dy[b, o], dW[out,in] += dy[B,out]^T @ x[B,in] and
@@ -51,23 +55,28 @@ __global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t bat
 // branches.  Each GEMM's own arithmetic is unchanged, so results are too.
 // Only from the device's own stream: on a branch's or a caller's stream the
 // one side stream would tie independent branches together.
-int colsum_into(vkc_device_t dev, const float* dy, float* db, int64_t batch, int64_t out_dim) {
+int colsum_into(vkc_device_t dev, const float* dy, float* db, int64_t batch, int64_t out_dim, int overwrite) {
   if (!db || out_dim <= 0) return VKC_OK;
   const unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
-  k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db);
+  k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db, overwrite);
   return vkc::check_launch("dense_backward db");
 }
 
+// `accumulate` = 0: dW and db are overwritten (beta = 0 for the weight GEMM)
+// instead of added to; the same values as adding into zeroed gradients,
+// without the zeroing pass.
 int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy, float* dx,
-                         float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
+                         float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim, int accumulate = 1) {
+  const float wbeta = accumulate ? 1.0f : 0.0f;
+  const int overwrite = accumulate ? 0 : 1;
   if (dw && dx && dev->side_stream && dev->stream == dev->own_stream) {
     cudaStream_t main = dev->stream;
     VKC_CUDA(cudaEventRecord(dev->side_fork, main));
     VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->side_fork, 0));
     dev->stream = dev->side_stream;
-    int r = colsum_into(dev, dy, db, batch, out_dim);
+    int r = colsum_into(dev, dy, db, batch, out_dim, overwrite);
     if (r == VKC_OK)
-      r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw,
+      r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, wbeta, dw,
                    in_dim, vkc::GemmEpilogue{});
     dev->stream = main;
     // the join is recorded even after an error, so a capture stays joined
@@ -79,10 +88,10 @@ int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const 
     if (e != cudaSuccess && r == VKC_OK) r = vkc::set_error(VKC_ERR_CUDA, "side stream join: %s", cudaGetErrorString(e));
     return r;
   }
-  int r = colsum_into(dev, dy, db, batch, out_dim);
+  int r = colsum_into(dev, dy, db, batch, out_dim, overwrite);
   if (r != VKC_OK) return r;
   if (dw) {
-    r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, 1.0f, dw, in_dim,
+    r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, wbeta, dw, in_dim,
                  vkc::GemmEpilogue{});
     if (r != VKC_OK) return r;
   }
@@ -121,15 +130,12 @@ k_softmax(const float* x, float* y, int64_t rows, int64_t cols) {
   for (int64_t c = lane; c < cols; c += 32) yr[c] = expf(xr[c] - m) / s;
 }
 
-// loss_rows[r] = sum_c -y * log(p + 1e-8), p = softmax(x) or x.
-__global__ void __launch_bounds__(kThreads)
-k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, int64_t rows, int64_t cols,
-                int softmax) {
+// One row of cross entropy, called by one whole warp: returns (in every
+// lane) sum_c -y * log(p + 1e-8) with p = softmax(x) (or x), storing p and,
+// when dx is given, the softmax-cross-entropy gradient (p - y) * gscale.
+__device__ __forceinline__ float ce_row(const float* xr, const float* yr, float* pr, float* dxr, int64_t cols,
+                                        int softmax, float gscale) {
   const int lane = threadIdx.x & 31;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (r >= rows) return;
-  const float* xr = x + r * cols;
-  const float* yr = y + r * cols;
   float m = 0.f, s = 1.f;
   if (softmax) {
     m = -INFINITY;
@@ -142,11 +148,49 @@ k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, 
   float L = 0.f;
   for (int64_t c = lane; c < cols; c += 32) {
     float p = softmax ? expf(xr[c] - m) / s : xr[c];
-    if (p_out) p_out[r * cols + c] = p;
+    if (pr) pr[c] = p;
+    if (dxr) dxr[c] = __fmul_rn(__fsub_rn(p, yr[c]), gscale);
     L += (-yr[c]) * logf(p + 1e-8f);
   }
-  L = warp_sum(L);
+  return warp_sum(L);
+}
+
+// loss_rows[r] = sum_c -y * log(p + 1e-8), p = softmax(x) or x (stored in
+// p_out when given); with dx, also the softmax-cross-entropy gradient
+// (p - y) * gscale.  One warp per row.
+__global__ void __launch_bounds__(kThreads)
+k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, float* dx, int64_t rows,
+                int64_t cols, int softmax, float gscale) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r >= rows) return;
+  const float L = ce_row(x + r * cols, y + r * cols, p_out ? p_out + r * cols : nullptr, dx ? dx + r * cols : nullptr,
+                         cols, softmax, gscale);
   if (lane == 0) loss_rows[r] = L;
+}
+
+// The batch reduction of the row losses with the arithmetic of the axis
+// reduction that ReduceLoss would launch for them (a (rows,) vector reduced
+// over axis 0: one thread in order up to 16 rows, one warp above, both
+// compensated sums), scaled by lscale.  One warp; rows <= kFusedCeMaxRows.
+constexpr int kFusedCeMaxRows = 2048;
+
+__global__ void __launch_bounds__(32) k_ce_batch_sum(const float* row_loss, float* loss, int64_t rows, float lscale) {
+  const int lane = threadIdx.x & 31;
+  Acc<VKC_SUM, true> acc;
+  acc.init();
+  if (rows <= 16) {
+    if (lane == 0) {
+      for (int64_t k = 0; k < rows; ++k) acc.push(row_loss[k]);
+      loss[0] = acc.value() * lscale;
+    }
+    return;
+  }
+  for (int64_t k = lane; k < rows; k += 32) acc.push(row_loss[k]);
+  warp_reduce(acc);
+  float v = __shfl_sync(0xffffffffu, acc.value(), 0);
+  v *= lscale;
+  if (lane == 0) loss[0] = v;
 }
 
 // The reference's Adam chain (optimizers.py:235-253), one element per step:
@@ -255,7 +299,7 @@ k_act_backward(const float* y, const float* dy, float* dx, size_t n) {
 // in shared memory; each thread issues its 2 x 32 loads before its stores.
 template <int ACT>
 __global__ void __launch_bounds__(256) k_act_colsum(const float* y, const float* dy_act, float* dy, int64_t batch,
-                                                    int64_t out_dim, float* db) {
+                                                    int64_t out_dim, float* db, int overwrite) {
   __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
   constexpr int kQ = vkc::kColsumRows / 8;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -289,7 +333,7 @@ __global__ void __launch_bounds__(256) k_act_colsum(const float* y, const float*
     }
     __syncthreads();
   }
-  if (db && w == 0 && in) db[c] += s;
+  if (db && w == 0 && in) db[c] = overwrite ? s : db[c] + s;
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -358,9 +402,10 @@ VKC_EXPORT int vkc_dense_backward(vkc_device_t dev, int precision, const float* 
   return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, db, batch, in_dim, out_dim);
 }
 
-VKC_EXPORT int vkc_dense_backward_act(vkc_device_t dev, int precision, const float* x, const float* w,
-                                      const float* dy_act, const float* y, int act, float* dy, float* dx, float* dw,
-                                      float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
+namespace {
+int dense_backward_act_any(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy_act,
+                           const float* y, int act, float* dy, float* dx, float* dw, float* db, int64_t batch,
+                           int64_t in_dim, int64_t out_dim, int accumulate) {
   VKC_BIND(dev);
   VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
   if (batch == 0) return VKC_OK;
@@ -368,14 +413,35 @@ VKC_EXPORT int vkc_dense_backward_act(vkc_device_t dev, int precision, const flo
   VKC_REQUIRE(act == VKC_ACT_RELU || act == VKC_ACT_SIGMOID, "activation %d has no backward kernel", act);
   if (out_dim > 0) {
     const unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
+    const int ow = accumulate ? 0 : 1;
     if (act == VKC_ACT_RELU)
-      k_act_colsum<VKC_ACT_RELU><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db);
+      k_act_colsum<VKC_ACT_RELU><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db, ow);
     else
-      k_act_colsum<VKC_ACT_SIGMOID><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db);
+      k_act_colsum<VKC_ACT_SIGMOID><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db, ow);
     const int r = vkc::check_launch("dense_backward_act dy, db");
     if (r != VKC_OK) return r;
   }
-  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, nullptr, batch, in_dim, out_dim);
+  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, nullptr, batch, in_dim, out_dim, accumulate);
+}
+}  // namespace
+
+VKC_EXPORT int vkc_dense_backward_act(vkc_device_t dev, int precision, const float* x, const float* w,
+                                      const float* dy_act, const float* y, int act, float* dy, float* dx, float* dw,
+                                      float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
+  return dense_backward_act_any(dev, precision, x, w, dy_act, y, act, dy, dx, dw, db, batch, in_dim, out_dim, 1);
+}
+
+VKC_EXPORT int vkc_dense_backward_ex(vkc_device_t dev, int precision, const float* x, const float* w,
+                                     const float* dy_act, const float* y, int act, float* dy, float* dx, float* dw,
+                                     float* db, int64_t batch, int64_t in_dim, int64_t out_dim, int accumulate) {
+  if (act != VKC_ACT_NONE)
+    return dense_backward_act_any(dev, precision, x, w, dy_act, y, act, dy, dx, dw, db, batch, in_dim, out_dim,
+                                  accumulate);
+  VKC_BIND(dev);
+  VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
+  if (batch == 0) return VKC_OK;
+  VKC_REQUIRE(x && w && dy_act, "NULL buffer");
+  return dense_backward_gemms(dev, precision, x, w, dy_act, dx, dw, db, batch, in_dim, out_dim, accumulate);
 }
 
 VKC_EXPORT int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols) {
@@ -393,8 +459,29 @@ VKC_EXPORT int vkc_cross_entropy(vkc_device_t dev, const float* x, const float* 
   if (rows <= 0) return VKC_OK;
   VKC_REQUIRE(x && y && loss_rows, "NULL buffer");
   unsigned grid = (unsigned)((rows * 32 + kThreads - 1) / kThreads);
-  k_cross_entropy<<<grid, kThreads, 0, dev->stream>>>(x, y, loss_rows, p_out, rows, cols, softmax);
+  k_cross_entropy<<<grid, kThreads, 0, dev->stream>>>(x, y, loss_rows, p_out, nullptr, rows, cols, softmax, 1.f);
   return vkc::check_launch("cross_entropy");
+}
+
+VKC_EXPORT int vkc_softmax_ce_fused(vkc_device_t dev, const float* x, const float* y, float* p_out, float* dx,
+                                    float* loss, int64_t rows, int64_t cols, float loss_scale, float grad_scale) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(rows >= 1 && rows <= kFusedCeMaxRows, "fused softmax cross entropy takes 1 to %d rows",
+              kFusedCeMaxRows);
+  VKC_REQUIRE(cols >= 1, "no classes");
+  VKC_REQUIRE(x && y && p_out && dx && loss, "NULL buffer");
+  float* row_loss = nullptr;
+  int r = vkc::scratch_alloc(dev, sizeof(float) * (size_t)rows, (void**)&row_loss);
+  if (r != VKC_OK) return r;
+  const unsigned grid = (unsigned)((rows * 32 + kThreads - 1) / kThreads);
+  k_cross_entropy<<<grid, kThreads, 0, dev->stream>>>(x, y, row_loss, p_out, dx, rows, cols, 1, grad_scale);
+  r = vkc::check_launch("softmax_ce_fused rows");
+  if (r == VKC_OK) {
+    k_ce_batch_sum<<<1, 32, 0, dev->stream>>>(row_loss, loss, rows, loss_scale);
+    r = vkc::check_launch("softmax_ce_fused batch sum");
+  }
+  vkc::scratch_free(dev, row_loss);
+  return r;
 }
 
 VKC_EXPORT int vkc_adam_update(vkc_device_t dev, float* value, const float* grad, float* m, float* v, size_t n,

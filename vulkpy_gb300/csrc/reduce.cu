@@ -16,6 +16,7 @@
 // values near 1 otherwise drift by ~0.1 ulp per factor); plain and pairwise
 // modes exist for the precision study.
 #include "common.cuh"
+#include "reduce_acc.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -23,87 +24,6 @@
 namespace {
 
 constexpr int kThreads = 256;
-
-template <int OP>
-__device__ __forceinline__ float identity() {
-  if constexpr (OP == VKC_SUM) return 0.f;
-  else if constexpr (OP == VKC_PROD) return 1.f;
-  else if constexpr (OP == VKC_MAXIMUM) return -INFINITY;
-  else return INFINITY;
-}
-
-template <int OP>
-__device__ __forceinline__ float combine(float a, float b) {
-  if constexpr (OP == VKC_SUM) return a + b;
-  else if constexpr (OP == VKC_PROD) return a * b;
-  else if constexpr (OP == VKC_MAXIMUM) return fmaxf(a, b);
-  else return fminf(a, b);
-}
-
-template <int OP>
-__device__ __forceinline__ double combine_d(double a, double b) {
-  if constexpr (OP == VKC_SUM) return a + b;
-  else if constexpr (OP == VKC_PROD) return a * b;
-  else if constexpr (OP == VKC_MAXIMUM) return fmax(a, b);
-  else return fmin(a, b);
-}
-
-// Accumulator: value s plus (for compensated sums) a running error term c.
-template <int OP, bool COMP>
-struct Acc {
-  float s, c;
-  __device__ __forceinline__ void init() { s = identity<OP>(); c = 0.f; }
-  __device__ __forceinline__ void push(float x) {
-    if constexpr (OP == VKC_SUM && COMP) {
-      // Neumaier's improvement of Kahan summation.
-      float t = s + x;
-      c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
-      s = t;
-    } else if constexpr (OP == VKC_PROD && COMP) {
-      // Compensated product (Graillat): the exact rounding error of s*x is
-      // fma(s, x, -p); c carries the accumulated error of the product.
-      float p = s * x;
-      float e = fmaf(s, x, -p);
-      c = fmaf(c, x, e);
-      s = p;
-    } else {
-      s = combine<OP>(s, x);
-    }
-  }
-  __device__ __forceinline__ void merge(float os, float oc) {
-    if constexpr (OP == VKC_SUM && COMP) {
-      // TwoSum of the leading parts; errors add into c.
-      float t = s + os;
-      float bp = t - s;
-      float err = (s - (t - bp)) + (os - bp);
-      s = t;
-      c = c + oc + err;
-    } else if constexpr (OP == VKC_PROD && COMP) {
-      // (s + c)(os + oc) ~ s*os + [err(s*os) + s*oc + c*os], then
-      // renormalise (Fast2Sum) so |c| stays below an ulp of s and the
-      // dropped c*oc term is negligible in long merge trees.
-      float p = s * os;
-      float e = fmaf(s, os, -p);
-      float cc = fmaf(s, oc, fmaf(c, os, e));
-      float t = p + cc;
-      c = cc - (t - p);
-      s = t;
-    } else {
-      s = combine<OP>(s, os);
-    }
-  }
-  __device__ __forceinline__ float value() const { return COMP ? s + c : s; }
-};
-
-template <int OP, bool COMP>
-__device__ __forceinline__ void warp_reduce(Acc<OP, COMP>& a) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    float os = __shfl_down_sync(0xffffffffu, a.s, o);
-    float oc = COMP ? __shfl_down_sync(0xffffffffu, a.c, o) : 0.f;
-    a.merge(os, oc);
-  }
-}
 
 // Block-wide reduction; result valid in thread 0.
 template <int OP, bool COMP>
@@ -649,9 +569,11 @@ VKC_EXPORT int vkc_reduce_axis(vkc_device_t dev, int op, const float* a, size_t 
 // be refused), and latency-critical paths where an allocation's possible
 // synchronisation or failure is not acceptable.  The block partials that
 // vkc_reduce_all takes from the memory pool live instead in a file-scope
-// device array of fixed size (1 MiB, 65536 partials), so one call handles at
-// most 65536 * 8192 = 2^29 elements and rejects larger inputs.  Every GPU
-// that loads this library holds the array until the process exits.
+// device array of fixed size (1 MiB, room for 65536 partials).  A call
+// launches the same grid as vkc_reduce_all (one block per 8192 elements, at
+// most 8 per SM), so the two entry points return the same bits; one call
+// accepts at most 65536 * 8192 = 2^29 elements and rejects larger inputs.
+// Every GPU that loads this library holds the array until the process exits.
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address (cudaGetSymbolAddress) and caches it; make that
@@ -688,7 +610,9 @@ int noalloc_partials(vkc_device_t dev, double** out) {
 
 template <int OP, bool COMP, int NACC>
 int reduce_all_noalloc_impl(vkc_device_t dev, const float* a, size_t n, float* out, float scale, double* partials) {
-  const size_t grid = (n + kNoAllocPerBlock - 1) / kNoAllocPerBlock;
+  const size_t want = (n + kNoAllocPerBlock - 1) / kNoAllocPerBlock;
+  const size_t grid = std::min<size_t>(std::max<size_t>(want, 1), (size_t)dev->sm_count * 8);
+  VKC_REQUIRE(grid <= kNoAllocMaxPartials, "vkc_reduce_all_noalloc: %zu partials exceed the scratch", grid);
   if (grid == 1) {
     k_reduce_all<OP, COMP, NACC><<<1, kThreads, 0, dev->stream>>>(a, n, nullptr, out, scale);
     return vkc::check_launch("reduce_all_noalloc");

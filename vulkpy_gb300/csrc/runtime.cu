@@ -13,7 +13,21 @@
 namespace vkc {
 
 std::atomic<uint64_t> g_launches{0};
+std::atomic<uint64_t> g_allocs{0};          // device + pinned host allocations requested
+std::atomic<int64_t> g_fail_alloc_in{-1};   // injected failure: fail when this reaches 0
 static thread_local std::string g_last_error;
+
+// Host-side fault injection (vkc_inject_alloc_failure): true when the
+// allocation being made now is the one chosen to fail.  Counts every
+// allocation request, injected or not.
+bool alloc_should_fail() {
+  g_allocs.fetch_add(1, std::memory_order_relaxed);
+  int64_t v = g_fail_alloc_in.load(std::memory_order_relaxed);
+  while (v >= 0) {
+    if (g_fail_alloc_in.compare_exchange_weak(v, v - 1, std::memory_order_relaxed)) return v == 0;
+  }
+  return false;
+}
 
 int set_error(int code, const char* fmt, ...) {
   char buf[1024];
@@ -42,6 +56,8 @@ int bind(vkc_device_t dev) {
 int scratch_alloc(vkc_device_t dev, size_t bytes, void** p) {
   *p = nullptr;
   if (bytes == 0) return VKC_OK;
+  if (alloc_should_fail())
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): injected allocation failure", bytes);
   cudaError_t e = cudaMallocAsync(p, bytes, dev->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -139,6 +155,8 @@ VKC_EXPORT int vkc_device_open(int index, float priority, vkc_device_t* out) {
   e = cudaStreamCreateWithPriority(&dev->own_stream, cudaStreamNonBlocking, prio);
   if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->copy_stream, cudaStreamNonBlocking, prio);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->copy_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->d2h_stream, cudaStreamNonBlocking, prio);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->d2h_after, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->side_stream, cudaStreamNonBlocking, prio);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->side_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->side_join, cudaEventDisableTiming);
@@ -168,11 +186,14 @@ VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
   cudaStreamSynchronize(dev->own_stream);
   if (dev->stream != dev->own_stream) cudaStreamSynchronize(dev->stream);
   cudaStreamSynchronize(dev->copy_stream);
+  cudaStreamSynchronize(dev->d2h_stream);
   if (dev->err_word) cudaFree(dev->err_word);
   if (dev->xo_jump_pows) cudaFree(dev->xo_jump_pows);
   if (dev->xo_next_pows) cudaFree(dev->xo_next_pows);
   cudaStreamSynchronize(dev->side_stream);
   cudaEventDestroy(dev->copy_done);
+  cudaEventDestroy(dev->d2h_after);
+  cudaStreamDestroy(dev->d2h_stream);
   cudaEventDestroy(dev->side_fork);
   cudaEventDestroy(dev->side_join);
   cudaStreamDestroy(dev->own_stream);
@@ -185,6 +206,7 @@ VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
 VKC_EXPORT int vkc_device_synchronize(vkc_device_t dev) {
   VKC_BIND(dev);
   VKC_CUDA(cudaStreamSynchronize(dev->copy_stream));
+  VKC_CUDA(cudaStreamSynchronize(dev->d2h_stream));
   VKC_CUDA(cudaStreamSynchronize(dev->stream));
   return VKC_OK;
 }
@@ -238,6 +260,8 @@ VKC_EXPORT int vkc_host_alloc(size_t bytes, void** ptr) {
   VKC_REQUIRE(ptr, "ptr is NULL");
   *ptr = nullptr;
   if (bytes == 0) return VKC_OK;
+  if (vkc::alloc_should_fail())
+    return set_error(VKC_ERR_OOM, "cudaHostAlloc(%zu bytes): injected allocation failure", bytes);
   cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -262,6 +286,8 @@ VKC_EXPORT int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void*
   VKC_CUDA(cudaStreamIsCapturing(dev->stream, &cap));
   VKC_REQUIRE(cap == cudaStreamCaptureStatusNone, "host uploads are not allowed while the stream is captured");
   std::lock_guard<std::mutex> lk(dev->mu);
+  if (vkc::alloc_should_fail())
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): injected allocation failure", bytes);
   // Allocate and copy on the copy stream so that the upload does not queue
   // behind compute work; the compute stream then waits for the copy.
   cudaError_t e = cudaMallocAsync(dptr, bytes, dev->copy_stream);
@@ -274,6 +300,72 @@ VKC_EXPORT int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void*
   VKC_CUDA(cudaEventRecord(dev->copy_done, dev->copy_stream));
   VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->copy_done, 0));
   VKC_CUDA(cudaEventSynchronize(dev->copy_done));
+  return VKC_OK;
+}
+
+namespace {
+// A job marking everything issued so far on `stream`.
+int record_on(vkc_device_t dev, cudaStream_t stream, vkc_job_t* job) {
+  auto* j = new vkc_job();
+  j->device = dev->index;
+  cudaError_t e = cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(j->ev, stream);
+  if (e != cudaSuccess) {
+    if (j->ev) cudaEventDestroy(j->ev);
+    delete j;
+    *job = nullptr;
+    return set_error(VKC_ERR_CUDA, "job record: %s", cudaGetErrorString(e));
+  }
+  *job = j;
+  return VKC_OK;
+}
+}  // namespace
+
+VKC_EXPORT int vkc_upload_async(vkc_device_t dev, const void* src, size_t bytes, void** dptr, vkc_job_t* job) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(dptr && job && (src || bytes == 0), "NULL argument");
+  *dptr = nullptr;
+  *job = nullptr;
+  if (bytes == 0) return VKC_OK;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VKC_CUDA(cudaStreamIsCapturing(dev->stream, &cap));
+  VKC_REQUIRE(cap == cudaStreamCaptureStatusNone, "host uploads are not allowed while the stream is captured");
+  std::lock_guard<std::mutex> lk(dev->mu);
+  if (vkc::alloc_should_fail())
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): injected allocation failure", bytes);
+  cudaError_t e = cudaMallocAsync(dptr, bytes, dev->copy_stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *dptr = nullptr;
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  VKC_CUDA(cudaMemcpyAsync(*dptr, src, bytes, cudaMemcpyHostToDevice, dev->copy_stream));
+  VKC_CUDA(cudaEventRecord(dev->copy_done, dev->copy_stream));
+  VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->copy_done, 0));
+  return record_on(dev, dev->copy_stream, job);
+}
+
+VKC_EXPORT int vkc_d2h_async(vkc_device_t dev, void* dst, const void* src, size_t bytes, vkc_job_t* job) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(job, "job is NULL");
+  *job = nullptr;
+  VKC_REQUIRE(dst && (src || bytes == 0), "NULL argument");
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VKC_CUDA(cudaStreamIsCapturing(dev->stream, &cap));
+  VKC_REQUIRE(cap == cudaStreamCaptureStatusNone, "host read-backs are not allowed while the stream is captured");
+  std::lock_guard<std::mutex> lk(dev->mu);
+  // after everything issued on the compute stream so far, not after what
+  // is issued later
+  VKC_CUDA(cudaEventRecord(dev->d2h_after, dev->stream));
+  VKC_CUDA(cudaStreamWaitEvent(dev->d2h_stream, dev->d2h_after, 0));
+  if (bytes) VKC_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, dev->d2h_stream));
+  return record_on(dev, dev->d2h_stream, job);
+}
+
+VKC_EXPORT int vkc_stream_wait_job(vkc_device_t dev, vkc_job_t job) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(job, "job is NULL");
+  VKC_CUDA(cudaStreamWaitEvent(dev->stream, job->ev, 0));
   return VKC_OK;
 }
 
@@ -382,6 +474,17 @@ VKC_EXPORT int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms) {
 VKC_EXPORT int vkc_launch_count(uint64_t* count) {
   VKC_REQUIRE(count, "count is NULL");
   *count = vkc::g_launches.load(std::memory_order_relaxed);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_alloc_count(uint64_t* count) {
+  VKC_REQUIRE(count, "count is NULL");
+  *count = vkc::g_allocs.load(std::memory_order_relaxed);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_inject_alloc_failure(int64_t after) {
+  vkc::g_fail_alloc_in.store(after < 0 ? -1 : after, std::memory_order_relaxed);
   return VKC_OK;
 }
 

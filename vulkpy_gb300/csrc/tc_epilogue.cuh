@@ -71,5 +71,39 @@ __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float
   __syncwarp();
 }
 
+// The same for an accumulator of the transposed product (a swapped
+// problem: TMEM lanes are columns of C, TMEM columns are rows of C).  acc:
+// this lane's column n0 + lane, rows m0 .. m0+31 of C; each store writes 32
+// consecutive columns of one row, so no shared-memory stage is needed.
+// Rows >= M and columns >= N are skipped.  All 32 lanes must call it.
+__device__ __forceinline__ void epilogue_tile32_t(const uint32_t (&acc)[32], float* C, const float* mask,
+                                                  const float* __restrict__ bias, int64_t ld, int n0, int N, int m0,
+                                                  int M, float alpha, float beta, int act) {
+  const int lane = threadIdx.x & 31;
+  const int col = n0 + lane;
+  const bool cin = col < N;
+  const int rows = min(32, M - m0);
+  const bool hb = bias != nullptr, hm = mask != nullptr, hc = beta != 0.f;
+  const float b = (hb && cin) ? bias[col] : 0.f;
+#pragma unroll
+  for (int j0 = 0; j0 < 32; j0 += 16) {
+    if (j0 >= rows) break;
+    float cv[16], mv[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int64_t off = (int64_t)(m0 + j0 + t) * ld + col;
+      const bool in = cin && j0 + t < rows;
+      cv[t] = (in && hc) ? C[off] : 0.f;
+      mv[t] = (in && hm) ? mask[off] : 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      if (cin && j0 + t < rows)
+        C[(int64_t)(m0 + j0 + t) * ld + col] =
+            epi_value(__uint_as_float(acc[j0 + t]), alpha, beta, cv[t], hb, b, act, hm, mv[t]);
+    }
+  }
+}
+
 }  // namespace
 }  // namespace vkc

@@ -55,17 +55,20 @@ class Dense(Module):
         y._written()
         return y
 
-    def backward(self, dy: Array, need_dx: bool = True) -> Array:
-        """Accumulate dW and db into the parameters' gradients and return dx
-        (not computed when ``need_dx`` is False, e.g. for the first layer)."""
+    def backward(self, dy: Array, need_dx: bool = True, accumulate: bool = True) -> Array:
+        """Accumulate dW and db into the parameters' gradients (with
+        ``accumulate`` False: overwrite them, as adding into zeroed gradients
+        would) and return dx (not computed when ``need_dx`` is False, e.g. for
+        the first layer)."""
         x = self._x
         dx = Array(dy._gpu, shape=(dy.shape[0], self.input_dim)) if need_dx else None
         wg = self.w.grad
         bg = self.b.grad
-        check(lib.vkc_dense_backward(
-            dy._h, _PREC[dy._gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy._dptr(),
-            dx._buf.ptr if dx is not None else None, wg._dptr() if wg is not None else None,
-            bg._dptr() if bg is not None else None, dy.shape[0], self.input_dim, self.output_dim))
+        check(lib.vkc_dense_backward_ex(
+            dy._h, _PREC[dy._gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy._dptr(), None,
+            _lib.ACT_NONE, None, dx._buf.ptr if dx is not None else None, wg._dptr() if wg is not None else None,
+            bg._dptr() if bg is not None else None, dy.shape[0], self.input_dim, self.output_dim,
+            1 if accumulate else 0))
         if wg is not None:
             wg._written()
         if bg is not None:
@@ -74,22 +77,24 @@ class Dense(Module):
             dx._written()
         return dx
 
-    def backward_act(self, dy_act: Array, act: int, y: Array, need_dx: bool = True) -> Array:
+    def backward_act(self, dy_act: Array, act: int, y: Array, need_dx: bool = True,
+                     accumulate: bool = True) -> Array:
         """The backward of the activation that follows this layer (output
         ``y``, gradient ``dy_act``) and then this layer's backward, with the
         activation derivative and the bias gradient in one kernel; the same
-        float32 results as the two ``backward`` calls."""
+        float32 results as the two ``backward`` calls.  ``accumulate`` as for
+        ``backward``."""
         x = self._x
         gpu = dy_act._gpu
         dy = Array(gpu, shape=(dy_act.shape[0], self.output_dim))
         dx = Array(gpu, shape=(dy_act.shape[0], self.input_dim)) if need_dx else None
         wg = self.w.grad
         bg = self.b.grad
-        check(lib.vkc_dense_backward_act(
+        check(lib.vkc_dense_backward_ex(
             dy_act._h, _PREC[gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy_act._dptr(), y._dptr(),
             act, dy._buf.ptr or 0, dx._buf.ptr if dx is not None else None,
             wg._dptr() if wg is not None else None, bg._dptr() if bg is not None else None,
-            dy_act.shape[0], self.input_dim, self.output_dim))
+            dy_act.shape[0], self.input_dim, self.output_dim, 1 if accumulate else 0))
         dy._written()
         if wg is not None:
             wg._written()

@@ -9,6 +9,8 @@ from __future__ import annotations
 
 from typing import Callable, Iterable, Literal, Optional, Tuple, cast
 
+import numpy as np
+
 from ..vkarray import Array
 from .._lib import lib, check
 from .core import Loss
@@ -76,11 +78,45 @@ class CrossEntropyLoss(ReduceLoss):
 
 
 class SoftmaxCrossEntropyLoss(CrossEntropyLoss):
-    """Cross entropy of softmax(x); dL/dx = softmax(x) - y (losses.py:179-249)."""
+    """Cross entropy of softmax(x); dL/dx = softmax(x) - y (losses.py:179-249).
+
+    For a 2-D batch of up to 2048 rows the loss step runs as two kernels:
+    row losses, softmax and the gradient that ``grad()`` then returns in the
+    first, their batch mean (or sum) in the second, with the same float32
+    results as the separate row-loss, reduction and gradient kernels."""
+
+    _FUSED_MAX_ROWS = 2048
 
     def __init__(self, *args, **kwargs):
         super().__init__(*args, **kwargs)
         self._sm = Softmax()
+        self._dx: Optional[Array] = None
+
+    def __call__(self, x: Array, y: Array) -> Array:
+        self._dx = None
+        if (len(x.shape) == 2 and tuple(y.shape) == tuple(x.shape)
+                and 1 <= x.shape[0] <= self._FUSED_MAX_ROWS and x.shape[1] >= 1):
+            self._x = x
+            self._y = y
+            rows = x.shape[0]
+            gpu = x._gpu
+            p = Array(gpu, shape=x.shape)
+            dx = Array(gpu, shape=x.shape)
+            loss = Array(gpu, shape=())
+            mean = self.scale_backward is not None
+            # ReduceLoss: mean(axis=0) scales by float32(1 / rows) in the
+            # reduction; grad() by the Python float 1 / rows
+            lscale = float(np.float32(1.0 / rows)) if mean else 1.0
+            gscale = self.scale_backward(dx) if mean else 1.0
+            check(lib.vkc_softmax_ce_fused(x._h, x._dptr(), y._dptr(), p._buf.ptr or 0, dx._buf.ptr or 0,
+                                           loss._buf.ptr or 0, rows, x.shape[1], lscale, float(gscale)))
+            for a in (p, dx, loss):
+                a._written()
+            self._sm._x = x
+            self._sm._y = p
+            self._dx = dx
+            return loss
+        return super().__call__(x, y)
 
     def forward(self, x: Array, y: Array) -> Array:
         if len(x.shape) == 2:
@@ -96,7 +132,10 @@ class SoftmaxCrossEntropyLoss(CrossEntropyLoss):
 
     def grad(self) -> Array:
         """(softmax(x) - y) * scale in one kernel: the same two float32 ops
-        as backward() followed by ReduceLoss's 1/batch scaling."""
+        as backward() followed by ReduceLoss's 1/batch scaling (already
+        computed by the fused loss step when that ran)."""
+        if self._dx is not None:
+            return self._dx
         p = cast(Array, self._sm._y)
         scale = 1.0 if self.scale_backward is None else self.scale_backward(p)
         dx = Array(p._gpu, shape=p.shape)

@@ -9,7 +9,7 @@ from ..vkarray import Array
 from ..graph import Graph
 from .._lib import lib, check
 from .core import Module, Loss
-from .layers import Dense, ReLU, Sigmoid
+from .layers import Dense, ReLU, Sigmoid, Softmax
 from .optimizers import AdamState, SGDState
 
 __all__ = ["Sequence", "CompiledStep"]
@@ -57,7 +57,10 @@ class Sequence:
             i += 1
         return x
 
-    def _backward(self):
+    def _backward(self, accumulate: bool = True):
+        """Backward through the layers; with ``accumulate`` False the Dense
+        layers overwrite their gradients (each is written once per step)
+        instead of adding to them."""
         dx = self.loss.grad()
         k = len(self.L) - 1
         while k >= 0:
@@ -67,14 +70,25 @@ class Sequence:
                     and getattr(layer, "_y", None) is not None
                     and len(dx.shape) == 2):
                 # the activation's backward and the Dense bias sum in one kernel
-                dx = prev.backward_act(dx, layer.act, layer._y, need_dx=k - 1 > 0)
+                dx = prev.backward_act(dx, layer.act, layer._y, need_dx=k - 1 > 0, accumulate=accumulate)
                 k -= 2
                 continue
-            if k == 0 and isinstance(layer, Dense):
+            if type(layer) is Dense:
+                dx = layer.backward(dx, need_dx=k > 0, accumulate=accumulate)
+            elif k == 0 and isinstance(layer, Dense):
                 layer.backward(dx, need_dx=False)
             else:
                 dx = layer.backward(dx)
             k -= 1
+
+    def _overwrites_grads(self) -> bool:
+        """True when one backward writes every gradient exactly once, so
+        train() can overwrite gradients instead of zeroing then adding:
+        only Dense / ReLU / Sigmoid / Softmax layers, no Dense twice."""
+        dense = [L for L in self.L if type(L) is Dense]
+        if len({id(L) for L in dense}) != len(dense):
+            return False
+        return all(type(L) in (Dense, ReLU, Sigmoid, Softmax) for L in self.L)
 
     def _params(self):
         """The trainable Parameters of the Dense layers, or None when another
@@ -148,11 +162,16 @@ class Sequence:
         return True
 
     def train(self, x: Array, y: Array) -> Tuple[Array, Array]:
-        """One step: forward, loss, zero_grad, backward, update (models.py:55-78)."""
+        """One step: forward, loss, zero_grad, backward, update (models.py:55-78).
+        When every gradient is written exactly once by the backward, the
+        zeroing is folded into it (gradients overwritten, the same values)."""
         _y = self._forward(x)
         _loss = self.loss(_y, y)
-        self._zero_grad()
-        self._backward()
+        if self.fuse and self._overwrites_grads():
+            self._backward(accumulate=False)
+        else:
+            self._zero_grad()
+            self._backward()
         self._update()
         return (_y, _loss)
 

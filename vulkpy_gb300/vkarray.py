@@ -88,6 +88,8 @@ class _Device:
             check(lib.vkc_device_check_errors(self.h, C.byref(flags)))
             if flags.value & 1:
                 raise IndexError("gather index out of range")
+            if flags.value & 2:
+                raise RuntimeError("tensor-core GEMM pipeline wait timed out")
         return Job(self, self.seq)
 
     def wait_seq(self, seq: int, timeout_ns: Optional[int] = None):
@@ -303,9 +305,24 @@ def empty_pinned(shape, dtype=np.float32) -> np.ndarray:
     """Uninitialised numpy array in pinned (page-locked) host memory.
 
     ``Array(gpu, data=a)`` from such an array uploads by DMA at full link
-    speed; the block returns to a pool when the array is garbage collected."""
+    speed and returns as soon as the copy is queued (the GPU's later ops on
+    the new array wait for it on the device): leave ``a`` unchanged until the
+    upload is done -- ``wait()`` on the new array, or any host access to
+    it, waits for that.  The block returns to a pool when the array is
+    garbage collected."""
     nbytes = max(1, int(np.prod(shape, dtype=np.int64))) * np.dtype(dtype).itemsize
     return np.asarray(_PinnedBlock(nbytes, tuple(shape), dtype))
+
+
+def _is_pinned(a: np.ndarray) -> bool:
+    """True when ``a``'s data lies in a block from ``empty_pinned``."""
+    b = a
+    while b is not None and not isinstance(b, _PinnedBlock):
+        b = getattr(b, "base", None)
+    if b is None:
+        return False
+    p = a.__array_interface__["data"][0]
+    return b.ptr <= p and p + a.nbytes <= b.ptr + b.cap
 
 
 def _host_buffer(shape, dtype) -> Tuple[np.ndarray, bool]:
@@ -324,14 +341,20 @@ class _DevBuf:
     same address on every launch, released when the graph is).  Frees of
     older buffers during a capture are deferred until it ends."""
 
-    __slots__ = ("dev", "ptr", "nbytes", "graph")
+    __slots__ = ("dev", "ptr", "nbytes", "graph", "h2d_job")
 
-    def __init__(self, dev: _Device, nbytes: int, src: Optional[np.ndarray] = None):
+    def __init__(self, dev: _Device, nbytes: int, src: Optional[np.ndarray] = None, pinned: bool = False):
         self.dev = dev
         self.nbytes = nbytes
         self.graph = dev.capture
+        self.h2d_job = None
         p = C.c_void_p()
-        if src is not None and nbytes > 0:
+        if src is not None and nbytes > 0 and pinned and self.graph is None:
+            # pinned source: queued on the copy stream, no host wait
+            j = C.c_void_p()
+            check(lib.vkc_upload_async(dev.h, src.ctypes.data, nbytes, C.byref(p), C.byref(j)))
+            self.h2d_job = j.value
+        elif src is not None and nbytes > 0:
             check(lib.vkc_upload(dev.h, src.ctypes.data, nbytes, C.byref(p)))
         else:
             check(lib.vkc_alloc(dev.h, nbytes, C.byref(p)))
@@ -388,13 +411,33 @@ class _GPUArray(Resource):
         self._host_valid = False
         self._dev_valid = True
         self._h2d_job = None  # raw job handle of a pending pinned upload
+        self._h2d_src = None  # the pinned source that upload reads
+        self._d2h_job = None  # raw job handle of a pending read-back (prefetch)
+        self._d2h_fresh = False  # no op has written the array since that read-back
 
     # -- construction helpers
     def _init_storage(self, shape, data: Optional[np.ndarray]):
         self.shape = tuple(int(s) for s in shape)
         self._size = _prod(self.shape)
         nbytes = self._size * 4  # float32 and uint32 elements
-        self._buf = _DevBuf(self._gpu._dev, nbytes, data)
+        pinned = data is not None and _is_pinned(data)
+        self._buf = _DevBuf(self._gpu._dev, nbytes, data, pinned)
+        if self._buf.h2d_job is not None:
+            self._h2d_job, self._h2d_src = self._buf.h2d_job, data
+
+    def __del__(self):
+        try:
+            if self._d2h_job is not None:
+                # the copy still writes into the host mirror: let it finish
+                # before the mirror can go back to the pinned pool
+                j, self._d2h_job = self._d2h_job, None
+                lib.vkc_job_wait(j, -1)
+                lib.vkc_job_destroy(j)
+            if self._h2d_job is not None:
+                lib.vkc_job_destroy(self._h2d_job)
+                self._h2d_job = None
+        except Exception:  # interpreter shutdown
+            pass
 
     # -- synchronisation
     def wait(self):
@@ -402,7 +445,41 @@ class _GPUArray(Resource):
         if self.job is not None:
             self.job.wait()
             self.job = None
+        self._wait_h2d()
         self._keep = []
+
+    def prefetch(self):
+        """Start copying this array to the host now, without waiting: the copy
+        runs after every op issued so far, on a separate stream, so it
+        overlaps the ops issued after it; a later host read (``np.asarray``,
+        indexing) then only waits for the copy.  No counterpart in the
+        reference, whose arrays live in host-visible memory."""
+        if self._host_valid or self._size == 0 or self._d2h_job is not None:
+            return
+        dev = self._gpu._dev
+        if dev.capture is not None:
+            return
+        self._ensure_device()
+        if self._host is None or not self._host_pinned:
+            self._host, self._host_pinned = np.asarray(_PinnedBlock(self._size * 4, self.shape, self._dtype)), True
+        elif self._host.shape != self.shape:
+            self._host = self._host.reshape(self.shape)
+        j = C.c_void_p()
+        check(lib.vkc_d2h_async(dev.h, self._host.ctypes.data, self._buf.ptr, self._buf.nbytes, C.byref(j)))
+        self._d2h_job = j.value
+        self._d2h_fresh = True
+
+    def _wait_d2h(self):
+        if self._d2h_job is not None:
+            j, self._d2h_job = self._d2h_job, None
+            try:
+                check(lib.vkc_job_wait(j, -1))
+            finally:
+                lib.vkc_job_destroy(j)
+            if self._d2h_fresh:
+                self._host_valid = True
+                self.job = None
+                self._keep = []
 
     def flush(self):
         """Upload pending host-side writes now."""
@@ -415,6 +492,7 @@ class _GPUArray(Resource):
                 check(lib.vkc_job_wait(j, -1))
             finally:
                 lib.vkc_job_destroy(j)
+                self._h2d_src = None
 
     def _ensure_device(self):
         """Make the device copy current (upload the host mirror if newer)."""
@@ -434,6 +512,7 @@ class _GPUArray(Resource):
 
     def _ensure_host(self) -> np.ndarray:
         """Make the host mirror current and return it."""
+        self._wait_d2h()
         if self._host is None:
             self._host, self._host_pinned = _host_buffer(self.shape, self._dtype)
             self._host_valid = False
@@ -466,6 +545,7 @@ class _GPUArray(Resource):
         """Record that an op on the stream (re)wrote this array."""
         self._dev_valid = True
         self._host_valid = False
+        self._d2h_fresh = False
         dev = self._gpu._dev
         if dev.capture is not None:
             dev.capture._touch(self, write=True)
