@@ -170,6 +170,13 @@ int vkc_timer_record(vkc_device_t dev, vkc_job_t* job);
 int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms);
 /* Number of kernels this library has launched since load (all devices). */
 int vkc_launch_count(uint64_t* count);
+/* Programmatic dependent launch for the kernels of the training step (the
+ * tensor-core GEMM, its operand pre-pass and split-K reduction, the Dense
+ * backward's bias sums, the loss step, the grouped Adam): each may be
+ * scheduled while the kernel before it on the stream finishes, and waits
+ * on the device for its results.  On by default; enable = 0 launches them
+ * as ordinary kernels.  No reference counterpart. */
+int vkc_set_pdl(int enable);
 /* Number of device and pinned-host allocations this library has requested
  * since load (vkc_alloc, vkc_upload, vkc_host_alloc and every scratch
  * allocation inside an op).  No reference counterpart; lets a caller check

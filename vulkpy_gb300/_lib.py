@@ -86,6 +86,7 @@ _SIGS = {
     "vkc_job_elapsed_ms": ([vp, vp, C.POINTER(C.c_float)], i32),
     "vkc_launch_count": ([C.POINTER(C.c_uint64)], i32),
     "vkc_alloc_count": ([C.POINTER(C.c_uint64)], i32),
+    "vkc_set_pdl": ([i32], i32),
     "vkc_inject_alloc_failure": ([i64], i32),
     "vkc_binary": ([vp, i32, vp, vp, vp, sz], i32),
     "vkc_binary_scalar": ([vp, i32, vp, f32, vp, sz], i32),

@@ -9,6 +9,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <utility>
 
 #include "../../include/vulkpy_gb300.h"
 
@@ -88,6 +89,36 @@ inline unsigned wave_grid(const vkc_device* dev, K* kernel, size_t work_items, i
 // Stream-ordered scratch allocation on the device's current stream.
 int scratch_alloc(vkc_device_t dev, size_t bytes, void** p);
 void scratch_free(vkc_device_t dev, void* p);
+
+// ---- programmatic dependent launch (PDL)
+// A kernel launched with launch_pdl may be scheduled while the kernel before
+// it on the stream is still running: its blocks become resident as that
+// kernel's blocks trigger (pdl_trigger) or exit, then wait in pdl_wait()
+// until it has completed and its memory is visible.  So the launch gap and
+// the block scheduling of consecutive short kernels overlap.  Every kernel
+// launched this way calls pdl_wait() before it touches global memory (after
+// it, everything the previous kernel wrote is visible, as after an ordinary
+// launch); without the launch attribute both calls are no-ops.
+extern std::atomic<int> g_pdl;  // 1: launch_pdl adds the attribute (vkc_set_pdl)
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_pdl.load(std::memory_order_relaxed) ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 }  // namespace vkc
 

@@ -138,6 +138,9 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
+  // the set-up above overlaps the previous kernel's tail; operands and C below
+  pdl_wait();
+  pdl_trigger();
 
   auto stage_a = [&](int s) { return base + s * Cfg::kStageBytes; };
   auto stage_b = [&](int s) { return stage_a(s) + Cfg::kABytes; };
@@ -428,6 +431,8 @@ struct SplitJob {
 __global__ void __launch_bounds__(256) k_split_pair(const __grid_constant__ SplitJob a,
                                                     const __grid_constant__ SplitJob b) {
   __shared__ float tile[64][65];
+  pdl_wait();
+  pdl_trigger();
   const bool first = blockIdx.x < a.blocks;
   const SplitJob& j = first ? a : b;
   const int64_t blk = first ? (int64_t)blockIdx.x : (int64_t)blockIdx.x - a.blocks;
@@ -457,7 +462,8 @@ int split_operands(vkc_device_t dev, const float* A, int64_t M, int64_t lda, boo
   const SplitJob ja = job(A, M, lda, a_kcontig, a_hi, a_lo), jb = job(B, N, ldb, b_kcontig, b_hi, b_lo);
   const int64_t grid = ja.blocks + jb.blocks;
   if (grid > 0x7fffffff) return set_error(VKC_ERR_INVALID, "matmul: operands too large for the pre-pass grid");
-  k_split_pair<<<(unsigned)grid, 256, 0, dev->stream>>>(ja, jb);
+  const cudaError_t e = launch_pdl(k_split_pair, dim3((unsigned)grid), dim3(256), 0, dev->stream, ja, jb);
+  if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "split_operands launch: %s", cudaGetErrorString(e));
   return check_launch("split_operands");
 }
 
@@ -563,6 +569,8 @@ __device__ __forceinline__ void add4(float4& s, const float4& a) {
 __global__ void __launch_bounds__(256)
 k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
                  float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t total = M * N, quads = total / 4;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += stride) {
@@ -597,6 +605,8 @@ k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64
 __global__ void __launch_bounds__(256)
 k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
                 float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t total = M * N;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
@@ -612,10 +622,14 @@ int splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M,
                   float* C, int64_t ldc, const GemmEpilogue& epi) {
   if (N % 4 == 0 && ldc % 4 == 0 && ((uintptr_t)C & 15u) == 0) {
     unsigned g = wave_grid(dev, k_splitk_reduce4, (size_t)(M * N / 4), 256);
-    k_splitk_reduce4<<<g, 256, 0, dev->stream>>>(partial, splits, M, N, alpha, beta, C, ldc, epi.bias, epi.act);
+    const cudaError_t e = launch_pdl(k_splitk_reduce4, dim3(g), dim3(256), 0, dev->stream, partial, splits, M, N,
+                                     alpha, beta, C, ldc, epi.bias, epi.act);
+    if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "splitk_reduce launch: %s", cudaGetErrorString(e));
   } else {
     unsigned g = stream_grid(dev, (size_t)(M * N), 256);
-    k_splitk_reduce<<<g, 256, 0, dev->stream>>>(partial, splits, M, N, alpha, beta, C, ldc, epi.bias, epi.act);
+    const cudaError_t e = launch_pdl(k_splitk_reduce, dim3(g), dim3(256), 0, dev->stream, partial, splits, M, N,
+                                     alpha, beta, C, ldc, epi.bias, epi.act);
+    if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "splitk_reduce launch: %s", cudaGetErrorString(e));
   }
   return check_launch("splitk_reduce");
 }
@@ -664,10 +678,11 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
     return set_error(VKC_ERR_INVALID, "matmul: too many output tiles");
   }
   const int ctas = (int)std::min<int64_t>(units, max_ctas(dev, kern, Cfg::kSmem));
-  kern<<<(unsigned)ctas, kThreadsP, Cfg::kSmem, dev->stream>>>(ma, mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta,
-                                                                 C, ldc, epi.bias, epi.act, dev->err_word, partial,
-                                                                 splits, kps, (int)m_blocks, n_blocks);
-  int r = check_launch("gemm_tc");
+  const cudaError_t e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kThreadsP), Cfg::kSmem, dev->stream, ma, mb, malo,
+                                   mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc, epi.bias, epi.act,
+                                   dev->err_word, partial, splits, kps, (int)m_blocks, n_blocks);
+  int r = e == cudaSuccess ? check_launch("gemm_tc")
+                           : set_error(VKC_ERR_CUDA, "gemm_tc launch: %s", cudaGetErrorString(e));
   if (r == VKC_OK && splits > 1) r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
   scratch_free(dev, partial);
   return r;

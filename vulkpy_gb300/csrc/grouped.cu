@@ -602,6 +602,8 @@ __device__ __forceinline__ void adam_elem(const AdamTable& tab, float d1, float 
 }
 
 __global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ AdamTable tab) {
+  pdl_wait();
+  pdl_trigger();
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
     int lo = 0, hi = tab.count - 1;
     while (lo < hi) {
@@ -1023,8 +1025,10 @@ VKC_EXPORT int vkc_adam_update_grouped(vkc_device_t dev, float* const* value, co
       total += I.chunks;  // an empty tensor still gets one chunk: its powers advance
     }
     tab.total = total;
-    k_adam_grouped<<<(unsigned)std::min<int>(total, dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
-    int r = check_launch("adam_grouped");
+    const cudaError_t e = launch_pdl(k_adam_grouped, dim3((unsigned)std::min<int>(total, dev->sm_count * 8)),
+                                     dim3(256), 0, dev->stream, tab);
+    int r = e == cudaSuccess ? check_launch("adam_grouped")
+                             : set_error(VKC_ERR_CUDA, "adam_grouped launch: %s", cudaGetErrorString(e));
     if (r != VKC_OK) return r;
   }
   return VKC_OK;

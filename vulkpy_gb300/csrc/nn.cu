@@ -41,6 +41,8 @@ int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64
 __global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t batch, int64_t out_dim, float* db,
                                                     int overwrite) {
   __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
+  vkc::pdl_wait();
+  vkc::pdl_trigger();
   const int64_t c0 = (int64_t)blockIdx.x * vkc::kColsumCols;
   const float s = vkc::colsum32(dy, batch, out_dim, out_dim, c0, tile);
   const int64_t o = c0 + threadIdx.x;
@@ -58,7 +60,9 @@ __global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t bat
 int colsum_into(vkc_device_t dev, const float* dy, float* db, int64_t batch, int64_t out_dim, int overwrite) {
   if (!db || out_dim <= 0) return VKC_OK;
   const unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
-  k_colsum_acc<<<grid, 256, 0, dev->stream>>>(dy, batch, out_dim, db, overwrite);
+  const cudaError_t e = vkc::launch_pdl(k_colsum_acc, dim3(grid), dim3(256), 0, dev->stream, dy, batch, out_dim, db,
+                                        overwrite);
+  if (e != cudaSuccess) return vkc::set_error(VKC_ERR_CUDA, "dense_backward db launch: %s", cudaGetErrorString(e));
   return vkc::check_launch("dense_backward db");
 }
 
@@ -161,6 +165,8 @@ __device__ __forceinline__ float ce_row(const float* xr, const float* yr, float*
 __global__ void __launch_bounds__(kThreads)
 k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, float* dx, int64_t rows,
                 int64_t cols, int softmax, float gscale) {
+  vkc::pdl_wait();
+  vkc::pdl_trigger();
   const int lane = threadIdx.x & 31;
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (r >= rows) return;
@@ -176,6 +182,8 @@ k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, 
 constexpr int kFusedCeMaxRows = 2048;
 
 __global__ void __launch_bounds__(32) k_ce_batch_sum(const float* row_loss, float* loss, int64_t rows, float lscale) {
+  vkc::pdl_wait();
+  vkc::pdl_trigger();
   const int lane = threadIdx.x & 31;
   Acc<VKC_SUM, true> acc;
   acc.init();
@@ -301,6 +309,8 @@ template <int ACT>
 __global__ void __launch_bounds__(256) k_act_colsum(const float* y, const float* dy_act, float* dy, int64_t batch,
                                                     int64_t out_dim, float* db, int overwrite) {
   __shared__ float tile[vkc::kColsumRows][vkc::kColsumCols + 1];
+  vkc::pdl_wait();
+  vkc::pdl_trigger();
   constexpr int kQ = vkc::kColsumRows / 8;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t c = (int64_t)blockIdx.x * vkc::kColsumCols + lane;
@@ -414,10 +424,14 @@ int dense_backward_act_any(vkc_device_t dev, int precision, const float* x, cons
   if (out_dim > 0) {
     const unsigned grid = (unsigned)((out_dim + vkc::kColsumCols - 1) / vkc::kColsumCols);
     const int ow = accumulate ? 0 : 1;
-    if (act == VKC_ACT_RELU)
-      k_act_colsum<VKC_ACT_RELU><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db, ow);
-    else
-      k_act_colsum<VKC_ACT_SIGMOID><<<grid, 256, 0, dev->stream>>>(y, dy_act, dy, batch, out_dim, db, ow);
+    const cudaError_t e =
+        act == VKC_ACT_RELU
+            ? vkc::launch_pdl(k_act_colsum<VKC_ACT_RELU>, dim3(grid), dim3(256), 0, dev->stream, y, dy_act, dy, batch,
+                              out_dim, db, ow)
+            : vkc::launch_pdl(k_act_colsum<VKC_ACT_SIGMOID>, dim3(grid), dim3(256), 0, dev->stream, y, dy_act, dy,
+                              batch, out_dim, db, ow);
+    if (e != cudaSuccess)
+      return vkc::set_error(VKC_ERR_CUDA, "dense_backward_act launch: %s", cudaGetErrorString(e));
     const int r = vkc::check_launch("dense_backward_act dy, db");
     if (r != VKC_OK) return r;
   }
@@ -474,11 +488,14 @@ VKC_EXPORT int vkc_softmax_ce_fused(vkc_device_t dev, const float* x, const floa
   int r = vkc::scratch_alloc(dev, sizeof(float) * (size_t)rows, (void**)&row_loss);
   if (r != VKC_OK) return r;
   const unsigned grid = (unsigned)((rows * 32 + kThreads - 1) / kThreads);
-  k_cross_entropy<<<grid, kThreads, 0, dev->stream>>>(x, y, row_loss, p_out, dx, rows, cols, 1, grad_scale);
-  r = vkc::check_launch("softmax_ce_fused rows");
+  cudaError_t e = vkc::launch_pdl(k_cross_entropy, dim3(grid), dim3(kThreads), 0, dev->stream, x, y, row_loss, p_out,
+                                  dx, rows, cols, 1, grad_scale);
+  r = e == cudaSuccess ? vkc::check_launch("softmax_ce_fused rows")
+                       : vkc::set_error(VKC_ERR_CUDA, "softmax_ce_fused launch: %s", cudaGetErrorString(e));
   if (r == VKC_OK) {
-    k_ce_batch_sum<<<1, 32, 0, dev->stream>>>(row_loss, loss, rows, loss_scale);
-    r = vkc::check_launch("softmax_ce_fused batch sum");
+    e = vkc::launch_pdl(k_ce_batch_sum, dim3(1), dim3(32), 0, dev->stream, row_loss, loss, rows, loss_scale);
+    r = e == cudaSuccess ? vkc::check_launch("softmax_ce_fused batch sum")
+                         : vkc::set_error(VKC_ERR_CUDA, "softmax_ce_fused launch: %s", cudaGetErrorString(e));
   }
   vkc::scratch_free(dev, row_loss);
   return r;

@@ -13,6 +13,7 @@
 namespace vkc {
 
 std::atomic<uint64_t> g_launches{0};
+std::atomic<int> g_pdl{1};
 std::atomic<uint64_t> g_allocs{0};          // device + pinned host allocations requested
 std::atomic<int64_t> g_fail_alloc_in{-1};   // injected failure: fail when this reaches 0
 static thread_local std::string g_last_error;
@@ -474,6 +475,11 @@ VKC_EXPORT int vkc_job_elapsed_ms(vkc_job_t start, vkc_job_t end, float* ms) {
 VKC_EXPORT int vkc_launch_count(uint64_t* count) {
   VKC_REQUIRE(count, "count is NULL");
   *count = vkc::g_launches.load(std::memory_order_relaxed);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_set_pdl(int enable) {
+  vkc::g_pdl.store(enable ? 1 : 0, std::memory_order_relaxed);
   return VKC_OK;
 }
 
