@@ -121,7 +121,7 @@ struct TileTable {
 // index is contiguous) into shared memory, then write 16-byte chunks of hi
 // (and lo = bf16(x - hi)) at their swizzled positions.  Rows >= rows and
 // k >= K are written as zeros.
-__global__ void __launch_bounds__(256) k_tile_operands(const __grid_constant__ TileTable tab) {
+__global__ void __launch_bounds__(256, 3) k_tile_operands(const __grid_constant__ TileTable tab) {
   __shared__ float s[kTileRows][kTileK + 1];
   const int tid = threadIdx.x;
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
@@ -130,21 +130,35 @@ __global__ void __launch_bounds__(256) k_tile_operands(const __grid_constant__ T
     const int rt = local / op.kt, kt = local % op.kt;
     const int64_t r0 = (int64_t)rt * kTileRows, k0 = (int64_t)kt * kTileK;
     __syncthreads();
+    // all 32 loads of a thread are issued before the shared-memory stores,
+    // so a tile waits for memory once
+    constexpr int kPer = kTileRows * kTileK / 256;
+    float v[kPer];
     if (op.k_contig) {
-#pragma unroll 4
-      for (int i = 0; i < kTileRows * kTileK / 256; ++i) {
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
         const int e = i * 256 + tid;
         const int r = e >> 6, k = e & 63;
         const int64_t gr = r0 + r, gk = k0 + k;
-        s[r][k] = (gr < op.rows && gk < op.k) ? op.src[gr * op.ld + gk] : 0.f;
+        v[i] = (gr < op.rows && gk < op.k) ? __ldg(op.src + gr * op.ld + gk) : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int e = i * 256 + tid;
+        s[e >> 6][e & 63] = v[i];
       }
     } else {
-#pragma unroll 4
-      for (int i = 0; i < kTileRows * kTileK / 256; ++i) {
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
         const int e = i * 256 + tid;
         const int k = e >> 7, r = e & 127;
         const int64_t gr = r0 + r, gk = k0 + k;
-        s[r][k] = (gr < op.rows && gk < op.k) ? op.src[gk * op.ld + gr] : 0.f;
+        v[i] = (gr < op.rows && gk < op.k) ? __ldg(op.src + gk * op.ld + gr) : 0.f;
+      }
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int e = i * 256 + tid;
+        s[e & 127][e >> 7] = v[i];
       }
     }
     __syncthreads();
@@ -666,41 +680,72 @@ __global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ Ad
 }
 
 // MSE gradient of the mean-reduced loss: ((x - y) * 2) * float32(1/batch),
-// the three float32 operations of MSELoss.backward and ReduceLoss.grad.
+// the three float32 operations of MSELoss.backward and ReduceLoss.grad.  A
+// thread's 16 elements of a chunk are loaded before any is stored.
 __global__ void __launch_bounds__(256) k_mse_grad_grouped(const __grid_constant__ VecTable tab) {
+  constexpr int kPer = kVecChunk / 256;
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
     const VecItem& I = tab.it[find_vec(tab, t)];
     const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
     const int64_t i1 = min(i0 + kVecChunk, I.n);
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += 256)
-      I.value[i] = __fmul_rn(__fmul_rn(__fsub_rn(I.grad[i], I.y[i]), 2.0f), I.scale);
+    float xv[kPer], yv[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int64_t i = i0 + u * 256 + threadIdx.x;
+      xv[u] = i < i1 ? I.grad[i] : 0.f;
+      yv[u] = i < i1 ? I.y[i] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int64_t i = i0 + u * 256 + threadIdx.x;
+      if (i < i1) I.value[i] = __fmul_rn(__fmul_rn(__fsub_rn(xv[u], yv[u]), 2.0f), I.scale);
+    }
   }
 }
 
 // MSE loss per model: mean over rows of sum over columns of (y - x)^2.  One
-// block per model; rows summed sequentially by column, the per-row sums
-// combined in a fixed tree.  (Not the order of the per-op path, whose
-// reduction kernels depend on the shape; the value agrees to rounding.)
-__global__ void __launch_bounds__(256) k_mse_loss_grouped(const __grid_constant__ VecTable tab, float* out) {
-  __shared__ float part[256];
+// block of 32 warps per model; a warp takes rows w, w + 32, ... with its
+// lanes along the columns (four rows' loads in flight), adds each row's
+// squares in a fixed shuffle tree, and keeps its rows' sums in order; the
+// warps' sums are then added in warp order.  (Not the order of the per-op
+// path, whose reduction kernels depend on the shape; the value agrees to
+// rounding.)
+constexpr int kMseWarps = 32;
+
+__global__ void __launch_bounds__(32 * kMseWarps) k_mse_loss_grouped(const __grid_constant__ VecTable tab, float* out) {
+  __shared__ float part[kMseWarps];
   const VecItem& I = tab.it[blockIdx.x];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t rows = I.n / I.cols;
   float acc = 0.f;
-  for (int64_t r = threadIdx.x; r < rows; r += 256) {
-    float s = 0.f;
-    for (int64_t c = 0; c < I.cols; ++c) {
-      const float d = __fsub_rn(I.y[r * I.cols + c], I.grad[r * I.cols + c]);
-      s = __fadd_rn(s, __fmul_rn(d, d));
+  for (int64_t r0 = w; r0 < rows; r0 += 4 * kMseWarps) {
+    float s[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int64_t c0 = 0; c0 < I.cols; c0 += 32) {
+      const int64_t c = c0 + lane;
+      float d[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t r = r0 + (int64_t)u * kMseWarps;
+        const bool in = r < rows && c < I.cols;
+        d[u] = in ? __fsub_rn(I.y[r * I.cols + c], I.grad[r * I.cols + c]) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s[u] = __fadd_rn(s[u], __fmul_rn(d[u], d[u]));
     }
-    acc += s;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
+      acc += s[u];
+    }
   }
-  part[threadIdx.x] = acc;
+  if (lane == 0) part[w] = acc;
   __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    float tot = 0.f;
+    for (int k = 0; k < kMseWarps; ++k) tot += part[k];
+    out[blockIdx.x] = tot * I.scale;
   }
-  if (threadIdx.x == 0) out[blockIdx.x] = part[0] * I.scale;
 }
 
 }  // namespace
@@ -967,7 +1012,7 @@ int vec_launch(vkc_device_t dev, int kind, float* const* value, const float* con
     } else if (kind == 1) {
       k_mse_grad_grouped<<<(unsigned)std::min<int>(std::max(total, 1), dev->sm_count * 8), 256, 0, dev->stream>>>(tab);
     } else {
-      k_mse_loss_grouped<<<(unsigned)tab.count, 256, 0, dev->stream>>>(tab, loss_out + s);
+      k_mse_loss_grouped<<<(unsigned)tab.count, 32 * kMseWarps, 0, dev->stream>>>(tab, loss_out + s);
     }
     int r = check_launch("grouped vector op");
     if (r != VKC_OK) return r;
