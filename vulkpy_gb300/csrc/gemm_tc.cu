@@ -299,7 +299,10 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
         tmem_ld32(tmem + lane_addr + (uint32_t)(b * BN + h * CW + c * 32), r0);
         const int col0 = p.n0 + h * CW + c * 32;
         if (p.m0 + q * 32 < M && col0 < N)
-          epilogue_tile32(r0, stage, cbase, nullptr, bias, ld, p.m0 + q * 32, M, col0, N, alpha, beta, act, raw_out);
+          // (the split kernel with 256-column tiles holds 128 running sums per
+          // thread and has no registers to spare for the fixed forms)
+          epilogue_tile32<!(X3 && BN == 256)>(r0, stage, cbase, nullptr, bias, ld, p.m0 + q * 32, M, col0, N, alpha,
+                                              beta, act, raw_out);
       }
       tc_fence_before();
       __syncwarp();

@@ -27,9 +27,74 @@ __device__ __forceinline__ float epi_value(float a, float alpha, float beta, flo
   return v;
 }
 
+// The common epilogues in fixed form: alpha == 1, beta == 0, act none or
+// ReLU, v = a (+ bias) (max 0) (* ReLU'(mask)).  With alpha == 1 the product
+// alpha * a is exact, so these give epi_value's results bit for bit whatever
+// the compiler contracts.  get(j) is this lane's value of row j; the lane
+// writes column `col` of rows row0 .. row0+rows-1 (rows <= 32) through a
+// pointer stepped by ld, so a value costs a load from the stage, the
+// arithmetic and a store (the general form re-derives every offset and
+// tests every flag per value).  The mask rows of each half are loaded
+// before its first store: one wait for memory per 16 rows.  (All 32 at once
+// does not fit the 168 registers a thread of a 10-warp CTA can have.)
+template <bool HB, bool RELU, bool HM, typename Get>
+__device__ __forceinline__ void epi_rows_fixed(Get get, float* C, const float* mask, float b, int64_t ld,
+                                               int64_t row0, int col, int rows) {
+  float* cp = C + row0 * ld + col;
+  const float* mp = HM ? mask + row0 * ld + col : nullptr;
+#pragma unroll
+  for (int h = 0; h < 32; h += 16) {
+    if (h >= rows) break;
+    float m[16];
+    if (HM) {
+#pragma unroll
+      for (int t = 0; t < 16; ++t) m[t] = h + t < rows ? mp[(h + t) * ld] : 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      if (h + t < rows) {
+        float v = get(h + t);
+        if (HB) v = v + b;
+        if (RELU) v = fmaxf(v, 0.f);
+        if (HM) v = relu_mask(v, m[t]);
+        *cp = v;
+      }
+      cp += ld;
+    }
+  }
+}
+
+// Picks the fixed form for the flags, or returns false (general form).
+template <typename Get>
+__device__ __forceinline__ bool epi_rows_dispatch(Get get, float* C, const float* mask, float b, int64_t ld,
+                                                  int64_t row0, int col, int rows, float alpha, float beta, int act,
+                                                  bool hb, bool hm, bool raw) {
+  if (raw) {
+    epi_rows_fixed<false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
+    return true;
+  }
+  if (alpha != 1.f || beta != 0.f || (act != VKC_ACT_NONE && act != VKC_ACT_RELU)) return false;
+  const bool relu = act == VKC_ACT_RELU;
+  if (!hm) {
+    if (!hb && !relu) epi_rows_fixed<false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
+    else if (hb && !relu) epi_rows_fixed<true, false, false>(get, C, nullptr, b, ld, row0, col, rows);
+    else if (hb && relu) epi_rows_fixed<true, true, false>(get, C, nullptr, b, ld, row0, col, rows);
+    else return false;
+    return true;
+  }
+  if (!hb && !relu) {
+    epi_rows_fixed<false, false, true>(get, C, mask, 0.f, ld, row0, col, rows);
+    return true;
+  }
+  return false;
+}
+
 // acc: this lane's row (row0 + lane), columns col0 .. col0+31.  C / mask
 // point at row 0 of the matrix (leading dimension ld); rows >= M and columns
-// >= N are skipped.  All 32 lanes must call it (warp-synchronous).
+// >= N are skipped.  All 32 lanes must call it (warp-synchronous).  FIXED:
+// use the fixed forms where the flags allow (a kernel short of registers
+// keeps only the general form).
+template <bool FIXED = true>
 __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float* __restrict__ stage, float* C,
                                                 const float* mask, const float* __restrict__ bias, int64_t ld,
                                                 int row0, int M, int col0, int N, float alpha, float beta, int act,
@@ -46,25 +111,33 @@ __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float
   const int rows = min(32, M - row0);
   const bool hb = bias != nullptr, hm = mask != nullptr, hc = beta != 0.f && !raw;
   const float b = (hb && cin) ? bias[col] : 0.f;
-  auto staged = [&](int j) { return stage[j * 32 + ((((lane >> 2) ^ j) & 7) << 2) + (lane & 3)]; };
+  // row j of the stage: chunk ((lane >> 2) ^ j) & 7, which repeats every 8 rows
+  int so[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) so[q] = ((((lane >> 2) ^ q) & 7) << 2) + (lane & 3);
+  auto staged = [&](int j) {
+    return FIXED ? stage[j * 32 + so[j & 7]] : stage[j * 32 + ((((lane >> 2) ^ j) & 7) << 2) + (lane & 3)];
+  };
+  if (FIXED && cin && epi_rows_dispatch(staged, C, mask, b, ld, row0, col, rows, alpha, beta, act, hb, hm, raw)) {
+  } else if (cin) {
 #pragma unroll 1
-  for (int j0 = 0; j0 < rows; j0 += 16) {
-    // the group's loads before its stores (a load after a store to C could
-    // not be hoisted: the pointers may alias); 16 rows per group, so a
-    // 32-row block waits for memory twice
-    float cv[16], mv[16];
+    for (int j0 = 0; j0 < rows; j0 += 16) {
+      // the group's loads before its stores (a load after a store to C could
+      // not be hoisted: the pointers may alias)
+      float cv[16], mv[16];
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      const int64_t off = (int64_t)(row0 + j0 + t) * ld + col;
-      const bool in = cin && j0 + t < rows;
-      cv[t] = (in && hc) ? C[off] : 0.f;
-      mv[t] = (in && hm) ? mask[off] : 0.f;
-    }
+      for (int t = 0; t < 16; ++t) {
+        const int64_t off = (int64_t)(row0 + j0 + t) * ld + col;
+        const bool in = j0 + t < rows;
+        cv[t] = (in && hc) ? C[off] : 0.f;
+        mv[t] = (in && hm) ? mask[off] : 0.f;
+      }
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      if (cin && j0 + t < rows) {
-        const float a = staged(j0 + t);
-        C[(int64_t)(row0 + j0 + t) * ld + col] = raw ? a : epi_value(a, alpha, beta, cv[t], hb, b, act, hm, mv[t]);
+      for (int t = 0; t < 16; ++t) {
+        if (j0 + t < rows) {
+          const float a = staged(j0 + t);
+          C[(int64_t)(row0 + j0 + t) * ld + col] = raw ? a : epi_value(a, alpha, beta, cv[t], hb, b, act, hm, mv[t]);
+        }
       }
     }
   }
@@ -85,6 +158,8 @@ __device__ __forceinline__ void epilogue_tile32_t(const uint32_t (&acc)[32], flo
   const int rows = min(32, M - m0);
   const bool hb = bias != nullptr, hm = mask != nullptr, hc = beta != 0.f;
   const float b = (hb && cin) ? bias[col] : 0.f;
+  auto reg = [&](int j) { return __uint_as_float(acc[j]); };
+  if (!cin || epi_rows_dispatch(reg, C, mask, b, ld, m0, col, rows, alpha, beta, act, hb, hm, false)) return;
 #pragma unroll
   for (int j0 = 0; j0 < 32; j0 += 16) {
     if (j0 >= rows) break;
@@ -92,13 +167,13 @@ __device__ __forceinline__ void epilogue_tile32_t(const uint32_t (&acc)[32], flo
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
       const int64_t off = (int64_t)(m0 + j0 + t) * ld + col;
-      const bool in = cin && j0 + t < rows;
+      const bool in = j0 + t < rows;
       cv[t] = (in && hc) ? C[off] : 0.f;
       mv[t] = (in && hm) ? mask[off] : 0.f;
     }
 #pragma unroll
     for (int t = 0; t < 16; ++t) {
-      if (cin && j0 + t < rows)
+      if (j0 + t < rows)
         C[(int64_t)(m0 + j0 + t) * ld + col] =
             epi_value(__uint_as_float(acc[j0 + t]), alpha, beta, cv[t], hb, b, act, hm, mv[t]);
     }
