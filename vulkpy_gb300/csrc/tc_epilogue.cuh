@@ -34,56 +34,76 @@ __device__ __forceinline__ float epi_value(float a, float alpha, float beta, flo
 // writes column `col` of rows row0 .. row0+rows-1 (rows <= 32) through a
 // pointer stepped by ld, so a value costs a load from the stage, the
 // arithmetic and a store (the general form re-derives every offset and
-// tests every flag per value).  The mask rows of each half are loaded
-// before its first store: one wait for memory per 16 rows.  (All 32 at once
-// does not fit the 168 registers a thread of a 10-warp CTA can have.)
-template <bool HB, bool RELU, bool HM, typename Get>
-__device__ __forceinline__ void epi_rows_fixed(Get get, float* C, const float* mask, float b, int64_t ld,
+// tests every flag per value).  All 32 mask rows are loaded before the
+// first store: one wait for memory per 32 rows.  (Stepped pointers keep
+// this within the 168 registers a thread of a 10-warp CTA can have; 32
+// offsets computed from the row index did not fit.)
+//
+// UPD (a parameter update fused into a gradient GEMM): v = a is stored as
+// the gradient and then value += scale * v, the SGD step with scale = -lr in
+// the arithmetic of the separate SGD kernels; `aux` is then the parameter
+// (same shape and leading dimension as C) and `b` the scale.  NR: rows per
+// call (the update form goes 16 rows at a time: its parameter rows and the
+// pointer to them would not fit the registers for 32).
+template <int NR, bool HB, bool RELU, bool HM, bool UPD, typename Get>
+__device__ __forceinline__ void epi_rows_fixed(Get get, float* C, const float* aux, float b, int64_t ld,
                                                int64_t row0, int col, int rows) {
   float* cp = C + row0 * ld + col;
-  const float* mp = HM ? mask + row0 * ld + col : nullptr;
+  float m[NR];
+  if (HM || UPD) {
+    const float* mp = aux + row0 * ld + col;
 #pragma unroll
-  for (int h = 0; h < 32; h += 16) {
-    if (h >= rows) break;
-    float m[16];
-    if (HM) {
-#pragma unroll
-      for (int t = 0; t < 16; ++t) m[t] = h + t < rows ? mp[(h + t) * ld] : 0.f;
+    for (int j = 0; j < NR; ++j) {
+      m[j] = j < rows ? *mp : 0.f;
+      mp += ld;
     }
+  }
+  float* up = UPD ? const_cast<float*>(aux) + row0 * ld + col : nullptr;
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      if (h + t < rows) {
-        float v = get(h + t);
-        if (HB) v = v + b;
-        if (RELU) v = fmaxf(v, 0.f);
-        if (HM) v = relu_mask(v, m[t]);
-        *cp = v;
-      }
-      cp += ld;
+  for (int j = 0; j < NR; ++j) {
+    if (j < rows) {
+      float v = get(j);
+      if (HB) v = v + b;
+      if (RELU) v = fmaxf(v, 0.f);
+      if (HM) v = relu_mask(v, m[j]);
+      *cp = v;
+      if (UPD) *up = __fadd_rn(m[j], __fmul_rn(b, v));
     }
+    cp += ld;
+    if (UPD) up += ld;
   }
 }
 
 // Picks the fixed form for the flags, or returns false (general form).
+// upd: the parameter of a fused update (nullptr: none), upd_scale its scale.
 template <typename Get>
 __device__ __forceinline__ bool epi_rows_dispatch(Get get, float* C, const float* mask, float b, int64_t ld,
                                                   int64_t row0, int col, int rows, float alpha, float beta, int act,
-                                                  bool hb, bool hm, bool raw) {
+                                                  bool hb, bool hm, bool raw, float* upd = nullptr,
+                                                  float upd_scale = 0.f) {
   if (raw) {
-    epi_rows_fixed<false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
+    epi_rows_fixed<32, false, false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
     return true;
   }
   if (alpha != 1.f || beta != 0.f || (act != VKC_ACT_NONE && act != VKC_ACT_RELU)) return false;
   const bool relu = act == VKC_ACT_RELU;
+  if (upd) {  // the host admits updates only on plain products
+    epi_rows_fixed<16, false, false, false, true>(get, C, upd, upd_scale, ld, row0, col, rows);
+    if (rows > 16) {
+      auto get_hi = [&](int j) { return get(j + 16); };
+      epi_rows_fixed<16, false, false, false, true>(get_hi, C, upd, upd_scale, ld, row0 + 16, col, rows - 16);
+    }
+    return true;
+  }
   if (!hm) {
-    if (!hb && !relu) epi_rows_fixed<false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
-    else if (hb && !relu) epi_rows_fixed<true, false, false>(get, C, nullptr, b, ld, row0, col, rows);
-    else if (hb && relu) epi_rows_fixed<true, true, false>(get, C, nullptr, b, ld, row0, col, rows);
+    if (!hb && !relu) epi_rows_fixed<32, false, false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
+    else if (hb && !relu) epi_rows_fixed<32, true, false, false, false>(get, C, nullptr, b, ld, row0, col, rows);
+    else if (hb && relu) epi_rows_fixed<32, true, true, false, false>(get, C, nullptr, b, ld, row0, col, rows);
     else return false;
     return true;
   }
   if (!hb && !relu) {
-    epi_rows_fixed<false, false, true>(get, C, mask, 0.f, ld, row0, col, rows);
+    epi_rows_fixed<32, false, false, true, false>(get, C, mask, 0.f, ld, row0, col, rows);
     return true;
   }
   return false;
@@ -98,7 +118,7 @@ template <bool FIXED = true>
 __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float* __restrict__ stage, float* C,
                                                 const float* mask, const float* __restrict__ bias, int64_t ld,
                                                 int row0, int M, int col0, int N, float alpha, float beta, int act,
-                                                bool raw) {
+                                                bool raw, float* upd = nullptr, float upd_scale = 0.f) {
   const int lane = threadIdx.x & 31;
   float4* srow = reinterpret_cast<float4*>(stage) + lane * 8;
 #pragma unroll
@@ -118,7 +138,8 @@ __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float
   auto staged = [&](int j) {
     return FIXED ? stage[j * 32 + so[j & 7]] : stage[j * 32 + ((((lane >> 2) ^ j) & 7) << 2) + (lane & 3)];
   };
-  if (FIXED && cin && epi_rows_dispatch(staged, C, mask, b, ld, row0, col, rows, alpha, beta, act, hb, hm, raw)) {
+  if (FIXED && cin &&
+      epi_rows_dispatch(staged, C, mask, b, ld, row0, col, rows, alpha, beta, act, hb, hm, raw, upd, upd_scale)) {
   } else if (cin) {
 #pragma unroll 1
     for (int j0 = 0; j0 < rows; j0 += 16) {
@@ -151,7 +172,8 @@ __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float
 // Rows >= M and columns >= N are skipped.  All 32 lanes must call it.
 __device__ __forceinline__ void epilogue_tile32_t(const uint32_t (&acc)[32], float* C, const float* mask,
                                                   const float* __restrict__ bias, int64_t ld, int n0, int N, int m0,
-                                                  int M, float alpha, float beta, int act) {
+                                                  int M, float alpha, float beta, int act, float* upd = nullptr,
+                                                  float upd_scale = 0.f) {
   const int lane = threadIdx.x & 31;
   const int col = n0 + lane;
   const bool cin = col < N;
@@ -159,7 +181,8 @@ __device__ __forceinline__ void epilogue_tile32_t(const uint32_t (&acc)[32], flo
   const bool hb = bias != nullptr, hm = mask != nullptr, hc = beta != 0.f;
   const float b = (hb && cin) ? bias[col] : 0.f;
   auto reg = [&](int j) { return __uint_as_float(acc[j]); };
-  if (!cin || epi_rows_dispatch(reg, C, mask, b, ld, m0, col, rows, alpha, beta, act, hb, hm, false)) return;
+  if (!cin || epi_rows_dispatch(reg, C, mask, b, ld, m0, col, rows, alpha, beta, act, hb, hm, false, upd, upd_scale))
+    return;
 #pragma unroll
   for (int j0 = 0; j0 < 32; j0 += 16) {
     if (j0 >= rows) break;
