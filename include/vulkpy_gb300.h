@@ -331,11 +331,36 @@ typedef struct vkc_gemm_problem {
  * vkc_gemm when that call does not split K; bf16: accumulated per 64-wide K
  * block in fp32 (at least as accurate as vkc_gemm's bf16). */
 int vkc_gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_problem* problems, int count);
+/* A parameter step fused into a grouped gradient GEMM: for every problem i
+ * with updates[i].value not NULL, after C is stored (the gradient, kept),
+ * value[r * ldc + c] += scale * C[r * ldc + c] -- the SGD step of
+ * optimizers.py:24-60 with scale = float(-lr), in the arithmetic of
+ * vkc_sgd_update_grouped, so the parameters equal a vkc_gemm_grouped call
+ * followed by that update bit for bit.  C and the value are contiguous
+ * m x n (ldc = n); such problems must be plain products (alpha 1, beta 0,
+ * no bias, activation or mask) whose own operands are not the value.  Other
+ * problems of the call may read the value as an operand and see it before
+ * the step (dx = dy W beside W's step).  `updates` may be NULL (then this is
+ * vkc_gemm_grouped).  The tensor-core path applies the step in the GEMM's
+ * epilogue when its problems fit one launch (128); otherwise, and on the
+ * fp32 path and for K = 0, one separate update runs after every product. */
+typedef struct vkc_gemm_update {
+  float* value;
+  float scale;
+} vkc_gemm_update;
+int vkc_gemm_grouped_update(vkc_device_t dev, int precision, const vkc_gemm_problem* problems,
+                            const vkc_gemm_update* updates, int count);
 /* db[i][o] += sum_b dy[i][b, o] for every item (the bias gradient of
  * layers.py:125-128), b in order, one launch per 128 items; with
  * `overwrite` db[i][o] = the sum (equal to accumulating into a zeroed db). */
 int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
                        const int64_t* cols, int count, int overwrite);
+/* vkc_colsum_grouped, then value[i][o] += scale[i] * db[i][o] in the same
+ * launch for every item whose value[i] is not NULL (the bias step of
+ * optimizers.py:24-60, arithmetic as in vkc_sgd_update_grouped). */
+int vkc_colsum_update_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
+                              const int64_t* cols, int count, int overwrite, float* const* value,
+                              const float* scale);
 /* value[i] += (-lr) * grad[i] for every tensor (optimizers.py:24-60). */
 int vkc_sgd_update_grouped(vkc_device_t dev, float* const* value, const float* const* grad, const int64_t* n,
                            double lr, int count);

@@ -233,3 +233,112 @@ def test_grouped_sequence_rejects_unsupported(gpu, vk):
     with pytest.raises(NotImplementedError):
         nn.GroupedSequence([nn.Sequence([nn.Dense(gpu, 3, 2, w_opt=nn.Adam(gpu), b_opt=nn.Adam(gpu))],
                                         nn.MSELoss())])
+
+
+def _update_pairs(vk, gpu, rng, shapes):
+    """For each (batch, in, out): dy (batch x out), x (batch x in), W (out x in):
+    dW = dy^T x with W's step fused, and dx = dy W, which reads W."""
+    host, dev = [], []
+    for b, i, o in shapes:
+        dy = rng.standard_normal((b, o)).astype(np.float32)
+        x = rng.standard_normal((b, i)).astype(np.float32)
+        W = rng.standard_normal((o, i)).astype(np.float32)
+        host.append((dy, x, W))
+        dev.append(tuple(vk.Array(gpu, data=a) for a in (dy, x, W)) +
+                   (vk.Array(gpu, shape=(o, i)), vk.Array(gpu, shape=(b, i))))
+    return host, dev
+
+
+def _pair_problems(lib_, shapes, dev):
+    probs = []
+    for (b, i, o), (dy, x, W, dW, dx) in zip(shapes, dev):
+        probs.append(lib_.GemmProblem(ta=1, tb=0, m=o, n=i, k=b, alpha=1.0, beta=0.0, a=dy._dptr(), lda=o,
+                                      b=x._dptr(), ldb=i, c=dW._dptr(), ldc=i, bias=None, act=0, relu_mask=None))
+        probs.append(lib_.GemmProblem(ta=0, tb=0, m=b, n=i, k=o, alpha=1.0, beta=0.0, a=dy._dptr(), lda=o,
+                                      b=W._dptr(), ldb=i, c=dx._dptr(), ldc=i, bias=None, act=0, relu_mask=None))
+    return probs
+
+
+@pytest.mark.parametrize("prec_name,pairs", [("fp32", 6), ("bf16", 6), ("bf16x3", 6), ("bf16x3", 70)])
+def test_grouped_fused_update(gpu, vk, prec_name, pairs):
+    """vkc_gemm_grouped_update: the gradients equal vkc_gemm_grouped's, dx
+    reads W before its step, and W ends at W + float32(-lr) * dW in the SGD
+    kernels' arithmetic -- in the epilogue (one launch) and through the
+    separate update (fp32, K = 0, and 140 problems: more than one launch)."""
+    from vulkpy_gb300 import _lib as lib_
+    prec = {"fp32": lib_.MM_FP32, "bf16": lib_.MM_BF16, "bf16x3": lib_.MM_BF16X3}[prec_name]
+    rng = np.random.default_rng(21)
+    shapes = [(37, 300, 50), (256, 1024, 20), (200, 129, 130), (1, 17, 2), (0, 40, 8), (64, 65, 64)]
+    while len(shapes) < pairs:
+        shapes.append((int(rng.integers(1, 300)), int(rng.integers(2, 300)), int(rng.integers(2, 100))))
+    shapes = shapes[:pairs]
+    host, dev = _update_pairs(vk, gpu, rng, shapes)
+    scale = np.float32(-0.01)
+    # the same products without updates, on copies of W
+    ref_dev = [(dy, x, vk.Array(gpu, data=h[2]), vk.Array(gpu, shape=dW.shape), vk.Array(gpu, shape=dx.shape))
+               for (dy, x, W, dW, dx), h in zip(dev, host)]
+    probs = _pair_problems(lib_, shapes, ref_dev)
+    assert lib_.lib.vkc_gemm_grouped(gpu.handle, prec, (lib_.GemmProblem * len(probs))(*probs), len(probs)) == 0
+    probs = _pair_problems(lib_, shapes, dev)
+    upds = []
+    for (dy, x, W, dW, dx) in dev:
+        upds += [lib_.GemmUpdate(value=W._dptr(), scale=float(scale)), lib_.GemmUpdate(value=None, scale=0.0)]
+    st = lib_.lib.vkc_gemm_grouped_update(gpu.handle, prec, (lib_.GemmProblem * len(probs))(*probs),
+                                          (lib_.GemmUpdate * len(upds))(*upds), len(probs))
+    assert st == 0, lib_.last_error()
+    for (dy, x, W, dW, dx), (_, _, _, rdW, rdx), h in zip(dev, ref_dev, host):
+        for a in (W, dW, dx, rdW, rdx):
+            a._written()
+        g = np.asarray(dW)
+        np.testing.assert_array_equal(g, np.asarray(rdW))
+        np.testing.assert_array_equal(np.asarray(dx), np.asarray(rdx))
+        np.testing.assert_array_equal(np.asarray(W), h[2] + scale * g)
+    assert gpu.check_errors() == 0
+
+
+def test_grouped_fused_update_rejects(gpu, vk):
+    from vulkpy_gb300 import _lib as lib_
+    rng = np.random.default_rng(3)
+    shapes = [(8, 16, 4)]
+    _, dev = _update_pairs(vk, gpu, rng, shapes)
+    dy, x, W, dW, dx = dev[0]
+    bias = vk.Array(gpu, data=np.ones(16, np.float32))
+    p = _pair_problems(lib_, shapes, dev)[0]
+    for field, value in (("bias", bias._dptr()), ("alpha", 2.0), ("act", 1)):
+        q = lib_.GemmProblem.from_buffer_copy(p)
+        setattr(q, field, value)
+        st = lib_.lib.vkc_gemm_grouped_update(gpu.handle, lib_.MM_BF16X3, C.byref(q),
+                                              C.byref(lib_.GemmUpdate(value=W._dptr(), scale=-0.1)), 1)
+        assert st != 0, field
+    # the value may not be the problem's own C or operand
+    st = lib_.lib.vkc_gemm_grouped_update(gpu.handle, lib_.MM_BF16X3, C.byref(p),
+                                          C.byref(lib_.GemmUpdate(value=x._dptr(), scale=-0.1)), 1)
+    assert st != 0
+
+
+def test_colsum_update_grouped(gpu, vk):
+    from vulkpy_gb300 import _lib as lib_
+    rng = np.random.default_rng(4)
+    shapes = [(5, 3), (256, 1024), (1, 40), (0, 7), (513, 65)]
+    dys = [rng.standard_normal(s).astype(np.float32) for s in shapes]
+    vals = [rng.standard_normal(s[1]).astype(np.float32) for s in shapes]
+    scales = np.array([-0.01, -0.5, -1e-3, -0.25, -2.0], np.float32)
+    d_dy = [vk.Array(gpu, data=d) if d.size else vk.Array(gpu, shape=d.shape) for d in dys]
+    d_db = [vk.Array(gpu, shape=(s[1],)) for s in shapes]
+    d_ref = [vk.Array(gpu, shape=(s[1],)) for s in shapes]
+    d_val = [vk.Array(gpu, data=v) for v in vals]
+    n = len(shapes)
+    ptrs = lambda arrs: (C.c_void_p * n)(*[a._dptr() for a in arrs])
+    rows = (C.c_int64 * n)(*[s[0] for s in shapes])
+    cols = (C.c_int64 * n)(*[s[1] for s in shapes])
+    assert lib_.lib.vkc_colsum_grouped(gpu.handle, ptrs(d_dy), ptrs(d_ref), rows, cols, n, 1) == 0
+    st = lib_.lib.vkc_colsum_update_grouped(gpu.handle, ptrs(d_dy), ptrs(d_db), rows, cols, n, 1, ptrs(d_val),
+                                            (C.c_float * n)(*scales))
+    assert st == 0, lib_.last_error()
+    for db, ref, v, v0, s in zip(d_db, d_ref, d_val, vals, scales):
+        for a in (db, ref, v):
+            a._written()
+        g = np.asarray(db)
+        np.testing.assert_array_equal(g, np.asarray(ref))
+        np.testing.assert_array_equal(np.asarray(v), v0 + s * g)
+    assert gpu.check_errors() == 0

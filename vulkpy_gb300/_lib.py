@@ -54,6 +54,11 @@ class GemmProblem(C.Structure):
                 ("b", C.c_void_p), ("ldb", C.c_int64), ("c", C.c_void_p), ("ldc", C.c_int64),
                 ("bias", C.c_void_p), ("act", C.c_int32), ("relu_mask", C.c_void_p)]
 
+
+class GemmUpdate(C.Structure):
+    """struct vkc_gemm_update (include/vulkpy_gb300.h)."""
+    _fields_ = [("value", C.c_void_p), ("scale", C.c_float)]
+
 _SIGS = {
     "vkc_last_error": ([], C.c_char_p),
     "vkc_version": ([], C.c_char_p),
@@ -106,7 +111,9 @@ _SIGS = {
     "vkc_gemm_tune_get": ([vp, i32, i64, i64, i64, C.POINTER(C.c_int)], i32),
     "vkc_gemm_tune_clear": ([], i32),
     "vkc_gemm_grouped": ([vp, i32, C.POINTER(GemmProblem), i32], i32),
+    "vkc_gemm_grouped_update": ([vp, i32, C.POINTER(GemmProblem), C.POINTER(GemmUpdate), i32], i32),
     "vkc_colsum_grouped": ([vp, pvp, pvp, pi64, pi64, i32, i32], i32),
+    "vkc_colsum_update_grouped": ([vp, pvp, pvp, pi64, pi64, i32, i32, pvp, C.POINTER(f32)], i32),
     "vkc_sgd_update_grouped": ([vp, pvp, pvp, pi64, f64, i32], i32),
     "vkc_adam_update_grouped": ([vp, pvp, pvp, pvp, pvp, pvp, pi64, i32, f64, f64, f64, f64], i32),
     "vkc_fill_f32_grouped": ([vp, pvp, pi64, f32, i32], i32),

@@ -210,6 +210,8 @@ struct TcProb {
   int swap;
   float alpha, beta;
   int act, tiles_n, tile0;
+  float* upd;  // parameter stepped by upd_scale * C in the epilogue (NULL: none)
+  float upd_scale;
 };
 
 __device__ __forceinline__ int tile_bn(const TcProb& P, int n0) {
@@ -443,10 +445,11 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
         if (P.swap) {
           // lanes are columns of C (kernel rows), TMEM columns rows of C
           if (m0 + q * 32 < P.n)
-            epilogue_tile32_t(r, P.c, P.mask, P.bias, P.ldc, m0 + q * 32, P.n, col0, P.m, P.alpha, P.beta, P.act);
+            epilogue_tile32_t(r, P.c, P.mask, P.bias, P.ldc, m0 + q * 32, P.n, col0, P.m, P.alpha, P.beta, P.act,
+                              P.upd, P.upd_scale);
         } else if (m0 + q * 32 < P.m) {
           epilogue_tile32(r, stage, P.c, P.mask, P.bias, P.ldc, m0 + q * 32, P.m, col0, P.n, P.alpha, P.beta, P.act,
-                          false);
+                          false, P.upd, P.upd_scale);
         }
       }
       tc_fence_before();
@@ -478,6 +481,8 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
 struct ColsumItem {
   const float* dy;
   float* db;
+  float* value;  // parameter stepped by scale * db (NULL: none)
+  float scale;
   int64_t batch, cols;
   int block0;  // first block of this item (blocks of 32 columns)
 };
@@ -488,7 +493,8 @@ struct ColsumTable {
 
 // db[o] += sum_b dy[b, o], b in order: the arithmetic of the single-layer
 // bias-gradient kernel.  `overwrite`: db[o] = the sum, which equals adding it
-// to a zeroed gradient (the sum starts at +0, so it is never -0).
+// to a zeroed gradient (the sum starts at +0, so it is never -0).  With a
+// value: value[o] += scale * db[o] (the SGD step's arithmetic).
 __global__ void __launch_bounds__(256) k_colsum_grouped(const __grid_constant__ ColsumTable tab) {
   __shared__ float tile[kColsumRows][kColsumCols + 1];
   for (int t = blockIdx.x; t < tab.total; t += gridDim.x) {
@@ -502,7 +508,11 @@ __global__ void __launch_bounds__(256) k_colsum_grouped(const __grid_constant__ 
     const int64_t c0 = (int64_t)(t - I.block0) * kColsumCols;
     const float s = colsum32(I.dy, I.batch, I.cols, I.cols, c0, tile);
     const int64_t o = c0 + threadIdx.x;
-    if (threadIdx.x < 32 && o < I.cols) I.db[o] = tab.overwrite ? s : I.db[o] + s;
+    if (threadIdx.x < 32 && o < I.cols) {
+      const float d = tab.overwrite ? s : I.db[o] + s;
+      I.db[o] = d;
+      if (I.value) I.value[o] = __fadd_rn(I.value[o], __fmul_rn(I.scale, d));
+    }
   }
 }
 
@@ -816,7 +826,8 @@ int grouped_simt(vkc_device_t dev, const vkc_gemm_problem* probs, const std::vec
   return VKC_OK;
 }
 
-int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const std::vector<int>& order) {
+int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const vkc_gemm_update* upd,
+               const std::vector<int>& order) {
   for (size_t s = 0; s < order.size(); s += kMaxGroup) {
     const size_t e = std::min(order.size(), s + kMaxGroup);
     // operand tile buffers: one allocation for the chunk
@@ -894,6 +905,8 @@ int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const s
       P.act = q.act;
       P.tiles_n = swap ? mt : nt;
       P.tile0 = total;
+      P.upd = upd ? upd[order[j]].value : nullptr;
+      P.upd_scale = upd ? upd[order[j]].scale : 0.f;
       total += mt * nt;
     }
     tt.total = ttotal;
@@ -930,8 +943,12 @@ int grouped_tc(vkc_device_t dev, bool x3, const vkc_gemm_problem* probs, const s
 
 }  // namespace
 
-VKC_EXPORT int vkc_gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_problem* problems, int count) {
-  VKC_BIND(dev);
+namespace {
+int vec_launch(vkc_device_t dev, int kind, float* const* value, const float* const* grad, const float* const* y,
+               const int64_t* n, const int64_t* cols, const float* scale, int count, float* loss_out);
+
+int gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_problem* problems, const vkc_gemm_update* updates,
+                 int count) {
   VKC_REQUIRE(count >= 0, "negative problem count");
   if (count == 0) return VKC_OK;
   VKC_REQUIRE(problems, "problems is NULL");
@@ -940,34 +957,71 @@ VKC_EXPORT int vkc_gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_
   for (int i = 0; i < count; ++i) {
     int r = check_problem(problems[i], i);
     if (r != VKC_OK) return r;
+    if (updates && updates[i].value) {
+      const vkc_gemm_problem& q = problems[i];
+      VKC_REQUIRE(q.alpha == 1.f && q.beta == 0.f && !q.bias && q.act == VKC_ACT_NONE && !q.relu_mask,
+                  "problem %d: a fused update needs a plain product (alpha 1, beta 0, no bias/act/mask)", i);
+      VKC_REQUIRE(q.ldc == q.n, "problem %d: a fused update needs a contiguous C (ldc = n)", i);
+      VKC_REQUIRE(updates[i].value != q.c && updates[i].value != q.a && updates[i].value != q.b,
+                  "problem %d: the updated value may not be C or an operand of its problem", i);
+    }
   }
   std::vector<int> order = work_order(problems, count);
-  if (precision == VKC_MM_FP32) return grouped_simt(dev, problems, order);
-  // K = 0 has no tensor-core work: C = act(beta*C + bias) through the SIMT path
   std::vector<int> tc, simt;
-  for (int i : order) (problems[i].k > 0 ? tc : simt).push_back(i);
+  // K = 0 has no tensor-core work: C = act(beta*C + bias) through the SIMT path
+  for (int i : order) (precision != VKC_MM_FP32 && problems[i].k > 0 ? tc : simt).push_back(i);
+  // Another problem may read an updated value as its operand (dx = dy W
+  // beside dW's step): the tensor-core path reads operands only in its
+  // tiling pass before the GEMM, so the step can run in the epilogue when all
+  // its problems go in one launch; the SIMT path reads them in the GEMM, so
+  // its steps (and those of a tensor-core call of several launches) run as
+  // one separate update after every product.
+  const bool fuse = updates && tc.size() <= (size_t)kMaxGroup;
   int r = grouped_simt(dev, problems, simt);
   if (r != VKC_OK) return r;
-  return grouped_tc(dev, precision == VKC_MM_BF16X3, problems, tc);
+  r = grouped_tc(dev, precision == VKC_MM_BF16X3, problems, fuse ? updates : nullptr, tc);
+  if (r != VKC_OK || !updates) return r;
+  std::vector<float*> val;
+  std::vector<const float*> grad;
+  std::vector<int64_t> n;
+  std::vector<float> scale;
+  auto add = [&](const std::vector<int>& ids) {
+    for (int i : ids) {
+      if (!updates[i].value) continue;
+      val.push_back(updates[i].value);
+      grad.push_back(problems[i].c);
+      n.push_back(problems[i].m * problems[i].n);
+      scale.push_back(updates[i].scale);
+    }
+  };
+  add(simt);
+  if (!fuse) add(tc);
+  if (val.empty()) return VKC_OK;
+  return vec_launch(dev, 0, val.data(), grad.data(), nullptr, n.data(), nullptr, scale.data(), (int)val.size(),
+                    nullptr);
 }
 
-VKC_EXPORT int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
-                                  const int64_t* cols, int count, int overwrite) {
-  VKC_BIND(dev);
+int colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
+                   const int64_t* cols, int count, int overwrite, float* const* value, const float* scale) {
   VKC_REQUIRE(count >= 0, "negative item count");
   if (count == 0) return VKC_OK;
   VKC_REQUIRE(dy && db && batch && cols, "NULL argument");
+  VKC_REQUIRE(!value || scale, "value without scale");
   for (int s = 0; s < count; s += kMaxGroup) {
     ColsumTable tab{};
     tab.overwrite = overwrite ? 1 : 0;
     int total = 0;
     for (int i = s; i < std::min(count, s + kMaxGroup); ++i) {
       VKC_REQUIRE(batch[i] >= 0 && cols[i] >= 0, "negative size");
-      if (cols[i] == 0 || (batch[i] == 0 && !overwrite)) continue;
+      float* v = value ? value[i] : nullptr;
+      if (cols[i] == 0 || (batch[i] == 0 && !overwrite && !v)) continue;
       VKC_REQUIRE((dy[i] || batch[i] == 0) && db[i], "NULL buffer");
+      VKC_REQUIRE(v != db[i], "value %d is its own gradient", i);
       ColsumItem& I = tab.it[tab.count++];
       I.dy = dy[i];
       I.db = db[i];
+      I.value = v;
+      I.scale = v ? scale[i] : 0.f;
       I.batch = batch[i];
       I.cols = cols[i];
       I.block0 = total;
@@ -980,6 +1034,31 @@ VKC_EXPORT int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, floa
     if (r != VKC_OK) return r;
   }
   return VKC_OK;
+}
+}  // namespace
+
+VKC_EXPORT int vkc_gemm_grouped(vkc_device_t dev, int precision, const vkc_gemm_problem* problems, int count) {
+  VKC_BIND(dev);
+  return gemm_grouped(dev, precision, problems, nullptr, count);
+}
+
+VKC_EXPORT int vkc_gemm_grouped_update(vkc_device_t dev, int precision, const vkc_gemm_problem* problems,
+                                       const vkc_gemm_update* updates, int count) {
+  VKC_BIND(dev);
+  return gemm_grouped(dev, precision, problems, updates, count);
+}
+
+VKC_EXPORT int vkc_colsum_update_grouped(vkc_device_t dev, const float* const* dy, float* const* db,
+                                         const int64_t* batch, const int64_t* cols, int count, int overwrite,
+                                         float* const* value, const float* scale) {
+  VKC_BIND(dev);
+  return colsum_grouped(dev, dy, db, batch, cols, count, overwrite, value, scale);
+}
+
+VKC_EXPORT int vkc_colsum_grouped(vkc_device_t dev, const float* const* dy, float* const* db, const int64_t* batch,
+                                  const int64_t* cols, int count, int overwrite) {
+  VKC_BIND(dev);
+  return colsum_grouped(dev, dy, db, batch, cols, count, overwrite, nullptr, nullptr);
 }
 
 namespace {

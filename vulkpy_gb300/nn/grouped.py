@@ -7,7 +7,10 @@ training step of a list of ``Sequence`` models -- each with its own layer
 widths and batch size -- as a handful of launches for all of them: one
 grouped GEMM per layer and direction (bias and ReLU fused into the forward
 epilogue, the ReLU derivative fused into the backward one), one grouped loss
-kernel, one grouped bias-gradient kernel per layer and one grouped SGD update.
+kernel and one grouped bias-gradient kernel per layer.  The SGD step is
+fused: each weight moves in the epilogue of the GEMM that computes its
+gradient and each bias in its gradient's column-sum kernel, after the
+gradient is stored and in the arithmetic of the separate SGD kernel.
 The step is graph-capturable (``Sequence.compile``-style: capture
 ``train(xs, ys)`` once and replay).
 
@@ -26,7 +29,7 @@ from typing import List, Sequence as Seq, Tuple
 import numpy as np
 
 from ..vkarray import Array
-from .._lib import lib, check, GemmProblem
+from .._lib import lib, check, GemmProblem, GemmUpdate
 from .. import _lib
 from .layers import Dense, ReLU
 from .losses import MSELoss
@@ -54,8 +57,6 @@ class GroupedSequence:
         if any(p != pattern[0] for p in pattern):
             raise ValueError("grouped models must have the same layer pattern")
         self.gpu = self.models[0].L[0].w.value._gpu
-        lrs = {st.opt.lr for p in self._plan for d, _ in p for st in (d.w.opt_state, d.b.opt_state)}
-        self._lrs = sorted(lrs)
 
     @staticmethod
     def _layers(model: Sequence):
@@ -81,9 +82,14 @@ class GroupedSequence:
             raise NotImplementedError("the last layer must be a Dense without activation")
         return out
 
-    def _gemm(self, problems: List[GemmProblem]):
+    def _gemm(self, problems: List[GemmProblem], updates: List[GemmUpdate] = None):
         arr = (GemmProblem * len(problems))(*problems)
-        check(lib.vkc_gemm_grouped(self.gpu._dev.h, _PREC[self.gpu.matmul_precision], arr, len(problems)))
+        if updates is None:
+            check(lib.vkc_gemm_grouped(self.gpu._dev.h, _PREC[self.gpu.matmul_precision], arr, len(problems)))
+        else:
+            upd = (GemmUpdate * len(updates))(*updates)
+            check(lib.vkc_gemm_grouped_update(self.gpu._dev.h, _PREC[self.gpu.matmul_precision], arr, upd,
+                                              len(problems)))
 
     def train(self, xs: Seq[Array], ys: Seq[Array]) -> Tuple[List[Array], Array]:
         """One step for every model: forward, MSE loss, backward, SGD.
@@ -130,12 +136,15 @@ class GroupedSequence:
         # ---- backward
         for l in range(nl - 1, -1, -1):
             dense = [self._plan[m][l][0] for m in range(n)]
-            # bias gradients (overwrite: db = 0 + sum_b dy)
-            check(lib.vkc_colsum_grouped(gpu._dev.h, _ptrs([dy._dptr() for dy in dys]),
-                                         _ptrs([d.b.grad._dptr() for d in dense]),
-                                         (C.c_int64 * n)(*[dy.shape[0] for dy in dys]),
-                                         (C.c_int64 * n)(*[d.output_dim for d in dense]), n, 1))
+            # bias gradients (overwrite: db = 0 + sum_b dy), then b += (-lr) db
+            check(lib.vkc_colsum_update_grouped(gpu._dev.h, _ptrs([dy._dptr() for dy in dys]),
+                                                _ptrs([d.b.grad._dptr() for d in dense]),
+                                                (C.c_int64 * n)(*[dy.shape[0] for dy in dys]),
+                                                (C.c_int64 * n)(*[d.output_dim for d in dense]), n, 1,
+                                                _ptrs([d.b.value._dptr() for d in dense]),
+                                                (C.c_float * n)(*[-d.b.opt_state.opt.lr for d in dense])))
             probs = []
+            upds = []
             nxt = []
             for m in range(n):
                 d = dense[m]
@@ -145,6 +154,8 @@ class GroupedSequence:
                     ta=1, tb=0, m=d.output_dim, n=d.input_dim, k=dy.shape[0], alpha=1.0, beta=0.0,
                     a=dy._dptr(), lda=d.output_dim, b=x._dptr(), ldb=d.input_dim, c=d.w.grad._dptr(),
                     ldc=d.input_dim, bias=None, act=_lib.ACT_NONE, relu_mask=None))
+                # then W += (-lr) dW in the same GEMM (its dx problem below reads W before the step)
+                upds.append(GemmUpdate(value=d.w.value._dptr(), scale=-d.w.opt_state.opt.lr))
                 if l > 0:
                     # dx = (dy W) * relu'(x): x is the previous layer's ReLU output
                     relu_prev = self._plan[m][l - 1][1]
@@ -155,21 +166,15 @@ class GroupedSequence:
                         a=dy._dptr(), lda=d.output_dim, b=d.w.value._dptr(), ldb=d.input_dim, c=dx._buf.ptr or 0,
                         ldc=d.input_dim, bias=None, act=_lib.ACT_NONE,
                         relu_mask=x._dptr() if relu_prev else None))
-            self._gemm(probs)
+                    upds.append(GemmUpdate(value=None, scale=0.0))
+            self._gemm(probs, upds)
             for d in dense:
                 d.w.grad._written()
                 d.b.grad._written()
+                d.w.value._written()
+                d.b.value._written()
             if l > 0:
                 for dx in nxt:
                     dx._written()
                 dys = nxt
-        # ---- SGD on every parameter, one launch per learning rate
-        for lr in self._lrs:
-            params = [p for plan in self._plan for d, _ in plan for p in (d.w, d.b) if p.opt_state.opt.lr == lr]
-            k = len(params)
-            check(lib.vkc_sgd_update_grouped(gpu._dev.h, _ptrs([p.value._dptr() for p in params]),
-                                             _ptrs([p.grad._dptr() for p in params]),
-                                             (C.c_int64 * k)(*[p.value._size for p in params]), float(lr), k))
-            for p in params:
-                p.value._written()
         return preds, losses
