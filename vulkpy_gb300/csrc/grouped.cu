@@ -214,6 +214,16 @@ struct TcProb {
   float upd_scale;
 };
 
+// L2 prefetch of columns [c0, c1) (at most 64) of row r: the first, the
+// 33rd and the last element's lines cover the span at any alignment.
+__device__ __forceinline__ void prefetch_seg_l2(const float* base, int64_t ld, int64_t r, int c0, int c1) {
+  if (c1 <= c0) return;
+  const float* p = base + r * ld;
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + c0));
+  if (c1 - c0 > 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + c0 + 32));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + c1 - 1));
+}
+
 __device__ __forceinline__ int tile_bn(const TcProb& P, int n0) {
   const int left = P.nk - n0;
   return left >= 128 ? 128 : ((left + 15) & ~15);
@@ -393,6 +403,18 @@ k_gemm_tc_grouped(const __grid_constant__ TcTable tab, uint32_t* err) {
       const int local = t - P.tile0;
       // kernel coordinates: rows m0 (TMEM lanes), columns n0 (TMEM columns)
       const int m0 = (local / P.tiles_n) * kTileRows, n0 = (local % P.tiles_n) * BN + hc * CW;
+      // The epilogue's second input (ReLU mask or the parameter of a fused
+      // update) does not depend on the accumulator: ask L2 for this warp's
+      // part of it now, so its loads after the wait find it there.
+      if (const float* aux = P.mask ? P.mask : P.upd) {
+        if (!P.swap) {
+          const int r = m0 + q * 32 + lane;
+          if (r < P.m) prefetch_seg_l2(aux, P.ldc, r, n0, min(n0 + CW, P.n));
+        } else {
+          const int c0 = m0 + q * 32, c1 = min(c0 + 32, P.n);
+          for (int r = n0 + lane; r < min(n0 + CW, P.m); r += 32) prefetch_seg_l2(aux, P.ldc, r, c0, c1);
+        }
+      }
       const int span = X3 ? kDrainX3 : P.kt;
       const int ngroups = (P.kt + span - 1) / span;
       float sum[X3 ? CW : 1];
