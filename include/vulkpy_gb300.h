@@ -177,6 +177,25 @@ int vkc_launch_count(uint64_t* count);
  * on the device for its results.  On by default; enable = 0 launches them
  * as ordinary kernels.  No reference counterpart. */
 int vkc_set_pdl(int enable);
+/* Split-K inside the tensor-core GEMM: when a product is split over 2..8 K
+ * ranges, the CTAs of one output tile run as a thread-block cluster, store
+ * their partial sums, meet on a cluster mbarrier and each adds up its share
+ * of the tile's rows (in K-range order, the same sums and epilogue as the
+ * separate reduction launch, so the same bits).  Used for launches outside
+ * a stream capture (inside a CUDA graph the separate reduction, overlapped
+ * by programmatic dependent launch, measured faster).  On by default;
+ * enable = 0 always uses the separate reduction launch.  No reference
+ * counterpart. */
+int vkc_set_cluster_splitk(int enable);
+/* The Dense backward (vkc_dense_backward*) runs the bias sum and the weight
+ * GEMM on branch streams forked from the device's stream and joins them back
+ * before it returns.  After vkc_side_defer(dev, 1) the joins wait: branches
+ * forked by later calls queue behind the earlier ones, and
+ * vkc_side_defer(dev, 0) joins them all back into the device's stream (the
+ * gradients are complete on it from then on).  A training step defers
+ * across its backward pass, so the weight GEMMs of every layer overlap the
+ * chain of input-gradient GEMMs.  No reference counterpart. */
+int vkc_side_defer(vkc_device_t dev, int defer);
 /* Number of device and pinned-host allocations this library has requested
  * since load (vkc_alloc, vkc_upload, vkc_host_alloc and every scratch
  * allocation inside an op).  No reference counterpart; lets a caller check
@@ -466,19 +485,34 @@ int vkc_dense_backward_ex(vkc_device_t dev, int precision, const float* x, const
                           const float* dy_act, const float* y, int act, float* dy, float* dx,
                           float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim,
                           int accumulate);
+/* vkc_dense_backward_ex with act VKC_ACT_NONE (dW, db from dy; accumulate as
+ * there), with the backward of the activation below this layer fused into
+ * the input-gradient GEMM: dx = (dy W) * act'(dx_y), dx_act VKC_ACT_RELU or
+ * VKC_ACT_SIGMOID and dx_y that activation's output (batch x in_dim), in the
+ * activation backward's float32 operations -- the dy of the Dense layer
+ * below, so the results equal vkc_dense_backward_ex then
+ * vkc_dense_backward_act's activation step bit for bit.  dx_act
+ * VKC_ACT_NONE: plain dx.  The tensor-core path applies the derivative in
+ * the GEMM's epilogue or split-K reduction (models.py:55-78 runs the two
+ * layers' backward one after the other). */
+int vkc_dense_backward_chain(vkc_device_t dev, int precision, const float* x, const float* w,
+                             const float* dy, const float* dx_y, int dx_act, float* dx, float* dw,
+                             float* db, int64_t batch, int64_t in_dim, int64_t out_dim, int accumulate);
 /* Row softmax over the last axis of [rows, cols] (nn/layers.py:297-300). */
 int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols);
 /* loss_rows[r] = sum_c -y log(p + 1e-8) with p = softmax(x) when softmax != 0
  * (else p = x); nn_cross_entropy.comp:21-26, losses.py:140-176, 218-249. */
 int vkc_cross_entropy(vkc_device_t dev, const float* x, const float* y, float* loss_rows,
                       float* p_out, int64_t rows, int64_t cols, int softmax);
-/* The softmax-cross-entropy loss step of one batch in two launches instead
+/* The softmax-cross-entropy loss step of one batch in one launch instead
  * of three (losses.py:179-249 with ReduceLoss, losses.py:40-92): p_out =
  * softmax(x) per row, dx = (p - y) * grad_scale, and *loss = (sum over rows
  * of sum_c -y log(p + 1e-8)) * loss_scale, the rows added with the
  * arithmetic of vkc_reduce_axis over a (rows,) vector, so the results equal
  * vkc_cross_entropy + vkc_reduce_axis + vkc_softmax_ce_backward bit for bit.
- * rows 1..2048. */
+ * rows 1..2048.  The last block of the launch adds up the rows (an arrival
+ * counter of the device, back at zero after each call): calls on one device
+ * must not run concurrently on different streams. */
 int vkc_softmax_ce_fused(vkc_device_t dev, const float* x, const float* y, float* p_out, float* dx,
                          float* loss, int64_t rows, int64_t cols, float loss_scale, float grad_scale);
 /* Adam step (optimizers.py:221-253) on n parameters, fused:

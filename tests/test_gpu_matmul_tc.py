@@ -124,3 +124,53 @@ def test_tile_widths_and_split_counts_agree(gpu, vk, m, n, k, prec, bound):
         from vulkpy_gb300 import autotune
         autotune.load_table()
     assert gpu.check_errors() == 0
+
+
+@pytest.mark.parametrize("m,n,k", [(256, 1024, 784), (256, 10, 1024), (129, 300, 700), (40, 520, 1100)])
+@pytest.mark.parametrize("prec", ["bf16x3", "bf16"])
+def test_cluster_splitk_matches_reduction_launch(gpu, vk, m, n, k, prec):
+    """Split-K reduced inside the GEMM by the CTAs of a cluster gives the bits
+    of the separate reduction launch (same sums in K-range order, same
+    epilogue), for 2..8 K ranges, tile widths 128 and 256, with bias,
+    activation and beta."""
+    import ctypes as C
+    from vulkpy_gb300 import _lib, autotune
+    P = {"bf16x3": _lib.MM_BF16X3, "bf16": _lib.MM_BF16}[prec]
+    rng = np.random.default_rng(m * 3 + n + k)
+    A = rng.standard_normal((m, k)).astype(np.float32)
+    B = rng.standard_normal((n, k)).astype(np.float32)
+    C0 = rng.standard_normal((m, n)).astype(np.float32)
+    bias = rng.standard_normal(n).astype(np.float32)
+    a, b, bb = vk.Array(gpu, data=A), vk.Array(gpu, data=B), vk.Array(gpu, data=bias)
+    exp = A.astype(np.float64) @ B.T.astype(np.float64)
+
+    def run(alpha, beta, with_bias, act):
+        c = vk.Array(gpu, data=C0)
+        if with_bias or act:
+            st = _lib.lib.vkc_dense_forward(gpu.handle, P, a._dptr(), b._dptr(), bb._dptr() if with_bias else None,
+                                            c._dptr(), m, k, n, act)
+        else:
+            st = _lib.lib.vkc_gemm(gpu.handle, P, 0, 1, m, n, k, C.c_float(alpha), a._dptr(), k, b._dptr(), k,
+                                   C.c_float(beta), c._dptr(), n)
+        assert st == 0, _lib.last_error()
+        c._written()
+        return np.asarray(c).copy()
+
+    try:
+        for tile in (128, 256):
+            for s in (2, 3, 5, 8):
+                assert _lib.lib.vkc_gemm_plan_set(P, m, n, k, s, tile) == 0
+                for args in ((1.0, 0.0, False, 0), (0.5, 2.0, False, 0), (1.0, 0.0, True, _lib.ACT_RELU),
+                             (1.0, 0.0, True, _lib.ACT_SIGMOID)):
+                    _lib.lib.vkc_set_cluster_splitk(1)
+                    got = run(*args)
+                    _lib.lib.vkc_set_cluster_splitk(0)
+                    ref = run(*args)
+                    np.testing.assert_array_equal(got, ref, err_msg=str((tile, s, args)))
+                    if args == (1.0, 0.0, False, 0):
+                        assert rel_fro(got, exp) < (1e-5 if prec == "bf16x3" else 8e-3)
+    finally:
+        _lib.lib.vkc_set_cluster_splitk(1)
+        _lib.lib.vkc_gemm_tune_set(P, m, n, k, 0)
+        autotune.load_table()
+    assert gpu.check_errors() == 0

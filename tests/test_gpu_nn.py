@@ -262,3 +262,48 @@ def test_grouped_parameter_update_matches_per_parameter(gpu, vk, optname, hidden
                 np.testing.assert_array_equal(np.asarray(pa.opt_state.v), np.asarray(pb.opt_state.v))
                 np.testing.assert_array_equal(np.asarray(pa.opt_state._powers), np.asarray(pb.opt_state._powers))
                 assert pa.opt_state.beta1t == pb.opt_state.beta1t
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "bf16x3"])
+@pytest.mark.parametrize("B,I,Out", [(256, 1024, 1024), (256, 1024, 10), (37, 300, 130)])
+def test_backward_chain_matches_backward_then_activation(gpu, vk, prec, B, I, Out):
+    """Dense.backward_chain (the activation derivative below the layer in the
+    input-gradient GEMM's epilogue or split-K reduction, in or outside a
+    cluster) gives the bits of Dense.backward followed by the activation's
+    own backward kernel, for ReLU and sigmoid, whole-K and split-K plans."""
+    from vulkpy_gb300 import _lib, autotune
+    from vulkpy_gb300.nn.layers import _act_backward
+    rng = np.random.default_rng(B + I + Out)
+    X = rng.standard_normal((B, I)).astype(f32)
+    DY = rng.standard_normal((B, Out)).astype(f32)
+    Yr = np.maximum(rng.standard_normal((B, I)), 0).astype(f32)
+    Yr[0, :5] = [0.0, -0.0, np.nan, 1e-30, -1e-30]
+    Ys = (1 / (1 + np.exp(-rng.standard_normal((B, I))))).astype(f32)
+    P = {"fp32": _lib.MM_FP32, "bf16": _lib.MM_BF16, "bf16x3": _lib.MM_BF16X3}[prec]
+    old = gpu.matmul_precision
+    gpu.matmul_precision = prec
+    try:
+        d = vk.nn.Dense(gpu, I, Out)
+        x = vk.Array(gpu, data=X)
+        d(x)
+        dy = vk.Array(gpu, data=DY)
+        for splits in (0, 1, 3, 8):
+            if splits:
+                _lib.lib.vkc_gemm_plan_set(P, B, I, Out, splits, 128)
+            for act, Yh in ((_lib.ACT_RELU, Yr), (_lib.ACT_SIGMOID, Ys)):
+                y = vk.Array(gpu, data=Yh)
+                for cl in (1, 0):
+                    _lib.lib.vkc_set_cluster_splitk(cl)
+                    got = np.asarray(d.backward_chain(dy, act, y, accumulate=False)).copy()
+                    gw, gb = np.asarray(d.w.grad).copy(), np.asarray(d.b.grad).copy()
+                    dx = d.backward(dy, accumulate=False)
+                    ref = np.asarray(_act_backward(act, y, dx)).copy()
+                    np.testing.assert_array_equal(got, ref, err_msg=str((splits, act, cl)))
+                    np.testing.assert_array_equal(gw, np.asarray(d.w.grad))
+                    np.testing.assert_array_equal(gb, np.asarray(d.b.grad))
+    finally:
+        gpu.matmul_precision = old
+        _lib.lib.vkc_set_cluster_splitk(1)
+        _lib.lib.vkc_gemm_tune_set(P, B, I, Out, 0)
+        autotune.load_table()
+    assert gpu.check_errors() == 0

@@ -92,6 +92,8 @@ _SIGS = {
     "vkc_launch_count": ([C.POINTER(C.c_uint64)], i32),
     "vkc_alloc_count": ([C.POINTER(C.c_uint64)], i32),
     "vkc_set_pdl": ([i32], i32),
+    "vkc_set_cluster_splitk": ([i32], i32),
+    "vkc_side_defer": ([vp, i32], i32),
     "vkc_inject_alloc_failure": ([i64], i32),
     "vkc_binary": ([vp, i32, vp, vp, vp, sz], i32),
     "vkc_binary_scalar": ([vp, i32, vp, f32, vp, sz], i32),
@@ -133,6 +135,7 @@ _SIGS = {
     "vkc_dense_backward": ([vp, i32, vp, vp, vp, vp, vp, vp, i64, i64, i64], i32),
     "vkc_dense_backward_act": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64], i32),
     "vkc_dense_backward_ex": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64, i32], i32),
+    "vkc_dense_backward_chain": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, i64, i64, i64, i32], i32),
     "vkc_softmax": ([vp, vp, vp, i64, i64], i32),
     "vkc_cross_entropy": ([vp, vp, vp, vp, vp, i64, i64, i32], i32),
     "vkc_adam_update": ([vp, vp, vp, vp, vp, sz, f64, f64, f64, f64, f64, f64], i32),

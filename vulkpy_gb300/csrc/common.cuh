@@ -26,8 +26,12 @@ struct vkc_device {
   cudaStream_t d2h_stream = nullptr;   // asynchronous read-backs (vkc_d2h_async)
   cudaEvent_t d2h_after = nullptr;     // reused marker: compute work a read-back follows
   cudaStream_t side_stream = nullptr;  // independent work forked from `stream` inside one call
-  cudaEvent_t side_fork = nullptr, side_join = nullptr;
+  cudaStream_t bias_stream = nullptr;  // a second such branch (the Dense backward's bias sums)
+  cudaEvent_t side_fork = nullptr, side_join = nullptr, bias_join = nullptr;
+  int side_defer = 0;    // vkc_side_defer: leave the branches open until vkc_side_defer(dev, 0)
+  int side_pending = 0;  // branches forked and not yet joined back
   uint32_t* err_word = nullptr;        // device error flags (bit0: gather index)
+  uint32_t* done_ctr = nullptr;        // arrival counter of last-block reductions (zero between kernels)
   uint32_t* xo_jump_pows = nullptr;    // xoshiro jump-map powers (lazy)
   uint32_t* xo_next_pows = nullptr;    // xoshiro next-map powers (lazy)
   std::mutex mu;
@@ -99,7 +103,8 @@ void scratch_free(vkc_device_t dev, void* p);
 // launched this way calls pdl_wait() before it touches global memory (after
 // it, everything the previous kernel wrote is visible, as after an ordinary
 // launch); without the launch attribute both calls are no-ops.
-extern std::atomic<int> g_pdl;  // 1: launch_pdl adds the attribute (vkc_set_pdl)
+extern std::atomic<int> g_pdl;             // 1: launch_pdl adds the attribute (vkc_set_pdl)
+extern std::atomic<int> g_cluster_splitk;  // 1: split-K reduced inside the GEMM (vkc_set_cluster_splitk)
 
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
@@ -117,6 +122,28 @@ inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = g_pdl.load(std::memory_order_relaxed) ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
+// launch_pdl with the blocks grouped into 1-D thread-block clusters of
+// `cluster` CTAs (grid.x a multiple of it).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl_cluster(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                                      unsigned cluster, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_pdl.load(std::memory_order_relaxed) ? 2 : 1;
   return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 

@@ -17,6 +17,11 @@ constexpr int kGemmBM = 128, kGemmBN = 128, kGemmBK = 16, kGemmThreads = 256;
 struct GemmEpilogue {
   const float* bias = nullptr;  // per output column, may be NULL
   int act = VKC_ACT_NONE;
+  // then v *= act'(dmask) for dact RELU / SIGMOID (dmask: the activation's
+  // output, C's layout): the backward of the activation below a Dense layer
+  // fused into the GEMM that computes its input gradient
+  const float* dmask = nullptr;
+  int dact = VKC_ACT_NONE;
 };
 
 struct SimtSmem {
@@ -30,6 +35,14 @@ __device__ __forceinline__ float relu_mask(float v, float y) {
   float s = y > 0.f ? 1.f : (y < 0.f ? -1.f : y);
   s = fmaxf(s, 0.f);
   return __fmul_rn(s, v);
+}
+
+// v times the derivative of the activation (ReLU or sigmoid) whose output is
+// y, in the float32 operations of the separate activation-backward kernel:
+// ReLU as relu_mask, sigmoid (1 - y) * y * v.
+__device__ __forceinline__ float act_deriv(float v, float y, int act) {
+  if (act == VKC_ACT_RELU) return relu_mask(v, y);
+  return __fmul_rn(__fmul_rn(__fsub_rn(1.0f, y), y), v);
 }
 
 // One 128 x 128 output tile at (m0, n0).  `mask` (may be NULL, same layout

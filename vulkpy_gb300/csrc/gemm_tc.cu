@@ -61,8 +61,9 @@ struct PCfg {
   static constexpr uint32_t kBBytes = BN * kBK * 2;
   static constexpr uint32_t kStageBytes = (X3 ? 2u : 1u) * (kABytes + kBBytes);
   static constexpr uint32_t kBarOff = STAGES * kStageBytes;
-  // full[S], empty[S], accf[2], acce[2], drain, then tmem slot + abort flag
-  static constexpr uint32_t kSlotOff = kBarOff + 8u * (2 * STAGES + 5);
+  // full[S], empty[S], accf[2], acce[2], drain, red[2], epi, then tmem slot
+  // + abort flag
+  static constexpr uint32_t kSlotOff = kBarOff + 8u * (2 * STAGES + 8);
   static constexpr uint32_t kEpiOff = (kSlotOff + 16 + 127) / 128 * 128;  // per-warp epilogue stages
   static constexpr uint32_t kSmem = kEpiOff + kEpiWarps * kEpiStageBytes + 1024 /*alignment slack*/;
 };
@@ -88,12 +89,56 @@ __device__ __forceinline__ PUnit unit_of(int u, int splits, int kps, int nk, int
   return p;
 }
 
+// C = act(alpha * sum_z partial[z] + beta * C + bias), z in order.
+__device__ __forceinline__ float splitk_epilogue(float s, float alpha, float beta, float c, bool has_bias, float bias,
+                                                 int act) {
+  float v = alpha * s;
+  if (beta != 0.f) v += beta * c;
+  if (has_bias) v += bias;
+  if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
+  else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
+  return v;
+}
+
+// Split-K inside a cluster: the cluster's `splits` CTAs have each stored the
+// partial sums of one K range of the tile (m0, n0) into partial[z] (M x N
+// planes); this CTA adds up rows [r0, r1) of the tile, z in order, and
+// writes them through the epilogue -- the arithmetic of the separate
+// reduction launch.  ew: the epilogue warp (0..7).
+__device__ __forceinline__ void cluster_reduce_rows(const float* partial, int splits, int M, int N, int m0, int n0,
+                                                    int bn, int r0, int r1, float alpha, float beta, float* C,
+                                                    int64_t ldc, const float* bias, int act, const float* dmask,
+                                                    int dact, int ew, int lane) {
+  const int64_t plane = (int64_t)M * N;
+  const int cols = min(bn, N - n0);
+  for (int r = r0 + ew; r < r1; r += kEpiWarps) {
+    const int64_t row = (int64_t)(m0 + r);
+    for (int c = lane; c < cols; c += 32) {
+      const int64_t off = row * N + n0 + c;
+      float t[8];
+#pragma unroll
+      for (int z = 0; z < 8; ++z) t[z] = z < splits ? __ldcg(partial + z * plane + off) : 0.f;
+      float s = t[0];
+#pragma unroll
+      for (int z = 1; z < 8; ++z)
+        if (z < splits) s += t[z];
+      float* cp = C + row * ldc + n0 + c;
+      float v = splitk_epilogue(s, alpha, beta, beta != 0.f ? *cp : 0.f, bias != nullptr, bias ? bias[n0 + c] : 0.f, act);
+      if (dmask) v = act_deriv(v, dmask[row * ldc + n0 + c], dact);
+      *cp = v;
+    }
+  }
+}
+
+// cl_reduce: the grid is made of clusters of `splits` CTAs (one per K range
+// of a tile) that reduce their partial sums themselves (no separate launch).
 template <bool X3, int BN, int STAGES, int DRAIN>
 __global__ void __launch_bounds__(kThreadsP, 1)
 k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
            const __grid_constant__ CUtensorMap map_alo, const __grid_constant__ CUtensorMap map_blo, int M, int N,
            int K, float alpha, float beta, float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-           uint32_t* err, float* __restrict__ partial, int splits, int kps, int m_blocks, int n_blocks) {
+           uint32_t* err, float* __restrict__ partial, int splits, int kps, int m_blocks, int n_blocks,
+           int cl_reduce, const float* __restrict__ dmask, int dact) {
   using Cfg = PCfg<X3, BN, STAGES>;
   constexpr uint32_t kCols = 2 * BN;  // two accumulators
   constexpr int CW = BN / 2;          // columns per epilogue warp
@@ -107,6 +152,11 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
   auto accf_bar = [&](int b) { return bars + 8u * (2 * STAGES + b); };
   auto acce_bar = [&](int b) { return bars + 8u * (2 * STAGES + 2 + b); };
   const uint32_t drain_bar = bars + 8u * (2 * STAGES + 4);
+  // red[u & 1]: all partials of the cluster's u-th tile stored (two, used in
+  // turn: a peer already on the next tile arrives on the other one, so it
+  // cannot complete a phase early); epi: this CTA's epilogue warps stored
+  auto red_bar = [&](int u) { return bars + 8u * (2 * STAGES + 5 + (u & 1)); };
+  const uint32_t epi_bar = bars + 8u * (2 * STAGES + 7);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + Cfg::kSlotOff);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
@@ -125,6 +175,11 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
       mbar_init(acce_bar(b), kEpiWarps);
     }
     mbar_init(drain_bar, 1);
+    if (cl_reduce) {
+      mbar_init(red_bar(0), (uint32_t)splits);  // one arrival from each CTA of the cluster
+      mbar_init(red_bar(1), (uint32_t)splits);
+      mbar_init(epi_bar, kEpiWarps);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -137,6 +192,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  // peers arrive on this CTA's red_bar only after every CTA has initialised it
+  if (cl_reduce) cluster_sync_all();
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
   // the set-up above overlaps the previous kernel's tail; operands and C below
   pdl_wait();
@@ -239,7 +296,7 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     const int q = warp & 3;          // TMEM lane quarter
     const int h = (warp - 2) >> 2;   // column half of the tile
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
-    int acc_it = 0;
+    int acc_it = 0, red_it = 0;
     bool ok = true;
     for (int u = (int)blockIdx.x; u < units && ok; u += (int)gridDim.x) {
       const PUnit p = unit_of<BN>(u, splits, kps, nk, m_blocks, n_blocks);
@@ -301,12 +358,38 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
         if (p.m0 + q * 32 < M && col0 < N)
           // (the split kernel with 256-column tiles holds 128 running sums per
           // thread and has no registers to spare for the fixed forms)
-          epilogue_tile32<!(X3 && BN == 256)>(r0, stage, cbase, nullptr, bias, ld, p.m0 + q * 32, M, col0, N, alpha,
-                                              beta, act, raw_out);
+          epilogue_tile32<!(X3 && BN == 256)>(r0, stage, cbase, raw_out ? nullptr : dmask, bias, ld, p.m0 + q * 32, M,
+                                              col0, N, alpha, beta, act, raw_out, nullptr, 0.f, dact);
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(acce_bar(b));
+      if (cl_reduce) {
+        // This warp's partial sums are stored; when all 8 warps' are, one
+        // thread tells every CTA of the cluster, and once all `splits` CTAs
+        // have, each adds up its share of the tile's rows.  (mbarriers with
+        // bounded waits, so a CTA that gave up cannot hang the others.)
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(epi_bar);
+        if (warp == 2 && lane == 0) {
+          if (mbar_wait(epi_bar, red_it & 1)) {
+            __threadfence();
+            for (int r = 0; r < splits; ++r) mbar_arrive_cluster(red_bar(red_it), (uint32_t)r);
+          } else {
+            ok = false;
+          }
+        }
+        if (!ok || !mbar_wait_cluster(red_bar(red_it), (red_it >> 1) & 1)) {
+          ok = false;
+          break;
+        }
+        ++red_it;
+        const int rows = min(kBM, M - p.m0), share = (kBM + splits - 1) / splits;
+        const int r0 = min(rows, p.z * share), r1 = min(rows, r0 + share);
+        cluster_reduce_rows(partial, splits, M, N, p.m0, p.n0, BN, r0, r1, alpha, beta, C, ldc, bias, act, dmask,
+                            dact, warp - 2, lane);
+      }
     }
     if (!ok) {
       if (lane == 0) atomicOr(err, 2u);
@@ -327,6 +410,8 @@ k_gemm_tcp(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CU
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
   }
+  // no CTA leaves while a peer may still arrive on its barriers
+  if (cl_reduce) cluster_sync_all();
 }
 
 // ------------------------------------------------------------ operand split
@@ -549,16 +634,6 @@ TcPlan choose_plan(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_
   return TcPlan{256, heuristic_splits(dev, cta_tiles(M, N, 256), nk)};
 }
 
-// C = act(alpha * sum_z partial[z] + beta * C + bias), z in order.
-__device__ __forceinline__ float splitk_epilogue(float s, float alpha, float beta, float c, bool has_bias, float bias,
-                                                 int act) {
-  float v = alpha * s;
-  if (beta != 0.f) v += beta * c;
-  if (has_bias) v += bias;
-  if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
-  else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-  return v;
-}
 
 __device__ __forceinline__ void add4(float4& s, const float4& a) {
   s.x += a.x;
@@ -571,7 +646,8 @@ __device__ __forceinline__ void add4(float4& s, const float4& a) {
 // the split loads are issued four at a time ahead of their (ordered) adds.
 __global__ void __launch_bounds__(256)
 k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
-                 float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
+                 float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
+                 const float* __restrict__ dmask, int dact) {
   pdl_wait();
   pdl_trigger();
   const int64_t total = M * N, quads = total / 4;
@@ -601,13 +677,21 @@ k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64
     v.y = splitk_epilogue(s.y, alpha, beta, c0.y, hb, b4.y, act);
     v.z = splitk_epilogue(s.z, alpha, beta, c0.z, hb, b4.z, act);
     v.w = splitk_epilogue(s.w, alpha, beta, c0.w, hb, b4.w, act);
+    if (dmask) {
+      const float4 y4 = *reinterpret_cast<const float4*>(dmask + r * ldc + col);
+      v.x = act_deriv(v.x, y4.x, dact);
+      v.y = act_deriv(v.y, y4.y, dact);
+      v.z = act_deriv(v.z, y4.z, dact);
+      v.w = act_deriv(v.w, y4.w, dact);
+    }
     *cp = v;
   }
 }
 
 __global__ void __launch_bounds__(256)
 k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
-                float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act) {
+                float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
+                const float* __restrict__ dmask, int dact) {
   pdl_wait();
   pdl_trigger();
   const int64_t total = M * N;
@@ -617,21 +701,23 @@ k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_
     for (int z = 1; z < splits; ++z) s += partial[(int64_t)z * total + i];
     const int64_t r = i / N, col = i - r * N;
     float* c = C + r * ldc + col;
-    *c = splitk_epilogue(s, alpha, beta, beta != 0.f ? *c : 0.f, bias != nullptr, bias ? bias[col] : 0.f, act);
+    float v = splitk_epilogue(s, alpha, beta, beta != 0.f ? *c : 0.f, bias != nullptr, bias ? bias[col] : 0.f, act);
+    if (dmask) v = act_deriv(v, dmask[r * ldc + col], dact);
+    *c = v;
   }
 }
 
 int splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M, int64_t N, float alpha, float beta,
                   float* C, int64_t ldc, const GemmEpilogue& epi) {
-  if (N % 4 == 0 && ldc % 4 == 0 && ((uintptr_t)C & 15u) == 0) {
+  if (N % 4 == 0 && ldc % 4 == 0 && ((uintptr_t)C & 15u) == 0 && ((uintptr_t)epi.dmask & 15u) == 0) {
     unsigned g = wave_grid(dev, k_splitk_reduce4, (size_t)(M * N / 4), 256);
     const cudaError_t e = launch_pdl(k_splitk_reduce4, dim3(g), dim3(256), 0, dev->stream, partial, splits, M, N,
-                                     alpha, beta, C, ldc, epi.bias, epi.act);
+                                     alpha, beta, C, ldc, epi.bias, epi.act, epi.dmask, epi.dact);
     if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "splitk_reduce launch: %s", cudaGetErrorString(e));
   } else {
     unsigned g = stream_grid(dev, (size_t)(M * N), 256);
     const cudaError_t e = launch_pdl(k_splitk_reduce, dim3(g), dim3(256), 0, dev->stream, partial, splits, M, N,
-                                     alpha, beta, C, ldc, epi.bias, epi.act);
+                                     alpha, beta, C, ldc, epi.bias, epi.act, epi.dmask, epi.dact);
     if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "splitk_reduce launch: %s", cudaGetErrorString(e));
   }
   return check_launch("splitk_reduce");
@@ -650,6 +736,33 @@ int max_ctas(vkc_device_t dev, Kern kern, uint32_t smem) {
   }
   cached = per_sm * dev->sm_count;
   return cached;
+}
+
+// Clusters of `size` CTAs of this kernel that can be resident at once (0: a
+// cluster launch is not possible), cached per instantiation and size.
+template <class Kern>
+int max_clusters(Kern kern, uint32_t smem, int size) {
+  static int cached[9] = {-1, -1, -1, -1, -1, -1, -1, -1, -1};
+  if (size < 2 || size > 8) return 0;
+  if (cached[size] >= 0) return cached[size];
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)size);
+  cfg.blockDim = dim3(kThreadsP);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)size;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, (const void*)kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  cached[size] = n;
+  return n;
 }
 
 template <bool X3, int BN, int STAGES, int DRAIN>
@@ -680,13 +793,38 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
     scratch_free(dev, partial);
     return set_error(VKC_ERR_INVALID, "matmul: too many output tiles");
   }
-  const int ctas = (int)std::min<int64_t>(units, max_ctas(dev, kern, Cfg::kSmem));
-  const cudaError_t e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kThreadsP), Cfg::kSmem, dev->stream, ma, mb, malo,
-                                   mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc, epi.bias, epi.act,
-                                   dev->err_word, partial, splits, kps, (int)m_blocks, n_blocks);
+  // 2..8 K ranges: the ranges of a tile run as one cluster and reduce in the
+  // kernel (units u = tile * splits + z go to CTA u mod grid, and a grid of
+  // whole clusters gives the CTAs of a cluster the splits of one tile).
+  // Only outside a stream capture: it saves a launch's host cost (MLP step
+  // eager 6.1k -> 6.4k steps/s), but in a CUDA graph the separate reduction,
+  // overlapped with the GEMM's tail by programmatic dependent launch, is
+  // faster (10.4k against 8.7k steps/s with the cluster form).
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(dev->stream, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;
+  }
+  const int clusters = splits > 1 && cap == cudaStreamCaptureStatusNone &&
+                               g_cluster_splitk.load(std::memory_order_relaxed)
+                           ? max_clusters(kern, Cfg::kSmem, splits)
+                           : 0;
+  cudaError_t e;
+  if (clusters > 0) {
+    const int ctas = (int)std::min<int64_t>(tiles, clusters) * splits;
+    e = launch_pdl_cluster(kern, dim3((unsigned)ctas), dim3(kThreadsP), Cfg::kSmem, dev->stream, (unsigned)splits, ma,
+                           mb, malo, mblo, (int)M, (int)N, (int)K, alpha, beta, C, ldc, epi.bias, epi.act,
+                           dev->err_word, partial, splits, kps, (int)m_blocks, n_blocks, 1, epi.dmask, epi.dact);
+  } else {
+    const int ctas = (int)std::min<int64_t>(units, max_ctas(dev, kern, Cfg::kSmem));
+    e = launch_pdl(kern, dim3((unsigned)ctas), dim3(kThreadsP), Cfg::kSmem, dev->stream, ma, mb, malo, mblo, (int)M,
+                   (int)N, (int)K, alpha, beta, C, ldc, epi.bias, epi.act, dev->err_word, partial, splits, kps,
+                   (int)m_blocks, n_blocks, 0, epi.dmask, epi.dact);
+  }
   int r = e == cudaSuccess ? check_launch("gemm_tc")
                            : set_error(VKC_ERR_CUDA, "gemm_tc launch: %s", cudaGetErrorString(e));
-  if (r == VKC_OK && splits > 1) r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
+  if (r == VKC_OK && splits > 1 && clusters == 0)
+    r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
   scratch_free(dev, partial);
   return r;
 }

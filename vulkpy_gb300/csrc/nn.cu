@@ -21,15 +21,43 @@ namespace {
 
 constexpr int kThreads = 256;
 
+template <int ACT>
+__device__ __forceinline__ float act_bwd(float yi, float dyi);
+
+template <int ACT>
+__global__ void __launch_bounds__(kThreads) k_act_backward(const float* y, const float* dy, float* dx, size_t n);
+
+// C *= act'(epi.dmask) elementwise after a GEMM that could not apply it in
+// its epilogue (C contiguous: ldc == N); in place, the separate
+// activation-backward kernel's arithmetic.
+int act_deriv_after(vkc_device_t dev, const vkc::GemmEpilogue& epi, float* C, int64_t M, int64_t N, int64_t ldc) {
+  if (epi.dact == VKC_ACT_NONE || M == 0 || N == 0) return VKC_OK;
+  VKC_REQUIRE(ldc == N, "activation derivative after a GEMM needs a contiguous C");
+  const size_t n = (size_t)(M * N);
+  const unsigned grid = vkc::stream_grid(dev, n, kThreads);
+  if (epi.dact == VKC_ACT_RELU)
+    k_act_backward<VKC_ACT_RELU><<<grid, kThreads, 0, dev->stream>>>(epi.dmask, C, C, n);
+  else
+    k_act_backward<VKC_ACT_SIGMOID><<<grid, kThreads, 0, dev->stream>>>(epi.dmask, C, C, n);
+  return vkc::check_launch("gemm activation derivative");
+}
+
+// The tensor-core GEMM applies epi.dmask/dact in its epilogue (or split-K
+// reduction); the GEMV and SIMT paths run the derivative as one more launch.
 int gemm_any(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
              const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
              vkc::GemmEpilogue epi) {
+  vkc::GemmEpilogue plain = epi;
+  plain.dmask = nullptr;
+  plain.dact = VKC_ACT_NONE;
   if (precision == VKC_MM_FP32 || precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3) {
-    const int r = vkc::gemm_as_gemv(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
-    if (r >= 0) return r;
+    const int r = vkc::gemm_as_gemv(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, plain);
+    if (r >= 0) return r == VKC_OK ? act_deriv_after(dev, epi, C, M, N, ldc) : r;
   }
-  if (precision == VKC_MM_FP32)
-    return vkc::gemm_simt(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
+  if (precision == VKC_MM_FP32 || ((precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3) && K == 0)) {
+    const int r = vkc::gemm_simt(dev, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, plain);
+    return r == VKC_OK ? act_deriv_after(dev, epi, C, M, N, ldc) : r;
+  }
   if (precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3)
     return vkc::gemm_tc(dev, precision, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, epi);
   return vkc::set_error(VKC_ERR_INVALID, "unknown matmul precision %d", precision);
@@ -51,10 +79,12 @@ __global__ void __launch_bounds__(256) k_colsum_acc(const float* dy, int64_t bat
 
 // db[o] += sum_b dy[b, o], dW[out,in] += dy[B,out]^T @ x[B,in] and
 // dx[B,in] = dy[B,out] @ W[out,in] (any may be NULL).  With dW and dx, the
-// bias sum and the weight GEMM run on the device's side stream, forked from the current stream and joined back before
-// returning, so the two independent GEMMs (and their operand splits and
-// split-K reductions) overlap; inside a graph capture they become parallel
-// branches.  Each GEMM's own arithmetic is unchanged, so results are too.
+// bias sum and the weight GEMM run on the device's side stream, forked from
+// the current stream and joined back before returning, so the two
+// independent GEMMs (and their operand splits and split-K reductions)
+// overlap; with dW and db only, the bias sum runs there beside the weight
+// GEMM.  Inside a graph capture these become parallel branches.  Each
+// kernel's own arithmetic is unchanged, so results are too.
 // Only from the device's own stream: on a branch's or a caller's stream the
 // one side stream would tie independent branches together.
 int colsum_into(vkc_device_t dev, const float* dy, float* db, int64_t batch, int64_t out_dim, int overwrite) {
@@ -70,26 +100,41 @@ int colsum_into(vkc_device_t dev, const float* dy, float* db, int64_t batch, int
 // instead of added to; the same values as adding into zeroed gradients,
 // without the zeroing pass.
 int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy, float* dx,
-                         float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim, int accumulate = 1) {
+                         float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim, int accumulate = 1,
+                         const float* dx_y = nullptr, int dx_act = VKC_ACT_NONE) {
+  vkc::GemmEpilogue dx_epi;
+  dx_epi.dmask = dx_y;
+  dx_epi.dact = dx_act;
   const float wbeta = accumulate ? 1.0f : 0.0f;
   const int overwrite = accumulate ? 0 : 1;
-  if (dw && dx && dev->side_stream && dev->stream == dev->own_stream) {
+  if (dw && (dx || db) && dev->side_stream && dev->stream == dev->own_stream) {
     cudaStream_t main = dev->stream;
     VKC_CUDA(cudaEventRecord(dev->side_fork, main));
     VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->side_fork, 0));
-    dev->stream = dev->side_stream;
+    VKC_CUDA(cudaStreamWaitEvent(dev->bias_stream, dev->side_fork, 0));
+    // bias stream: the bias sum; side stream: the weight GEMM when dx is
+    // wanted; main: dx, or the weight GEMM (the first layer has no dx)
+    dev->stream = dev->bias_stream;
     int r = colsum_into(dev, dy, db, batch, out_dim, overwrite);
-    if (r == VKC_OK)
+    dev->stream = dev->side_stream;
+    if (r == VKC_OK && dx)
       r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, wbeta, dw,
                    in_dim, vkc::GemmEpilogue{});
     dev->stream = main;
-    // the join is recorded even after an error, so a capture stays joined
-    cudaError_t e = cudaEventRecord(dev->side_join, dev->side_stream);
-    if (r == VKC_OK)
+    if (r == VKC_OK && dx)
       r = gemm_any(dev, precision, false, false, batch, in_dim, out_dim, 1.0f, dy, out_dim, w, in_dim, 0.0f, dx,
+                   in_dim, dx_epi);
+    else if (r == VKC_OK)
+      r = gemm_any(dev, precision, true, false, out_dim, in_dim, batch, 1.0f, dy, out_dim, x, in_dim, wbeta, dw,
                    in_dim, vkc::GemmEpilogue{});
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(main, dev->side_join, 0);
-    if (e != cudaSuccess && r == VKC_OK) r = vkc::set_error(VKC_ERR_CUDA, "side stream join: %s", cudaGetErrorString(e));
+    // joined back now, or (vkc_side_defer) when the caller ends the deferral,
+    // so the branches of several layers overlap the input-gradient chain; the
+    // join is recorded even after an error, so a capture stays joined
+    dev->side_pending = 1;
+    if (!dev->side_defer) {
+      const int rj = vkc_side_defer(dev, 0);
+      if (r == VKC_OK) r = rj;
+    }
     return r;
   }
   int r = colsum_into(dev, dy, db, batch, out_dim, overwrite);
@@ -101,7 +146,7 @@ int dense_backward_gemms(vkc_device_t dev, int precision, const float* x, const 
   }
   if (dx) {
     r = gemm_any(dev, precision, false, false, batch, in_dim, out_dim, 1.0f, dy, out_dim, w, in_dim, 0.0f, dx, in_dim,
-                 vkc::GemmEpilogue{});
+                 dx_epi);
   }
   return r;
 }
@@ -181,24 +226,48 @@ k_cross_entropy(const float* x, const float* y, float* loss_rows, float* p_out, 
 // compensated sums), scaled by lscale.  One warp; rows <= kFusedCeMaxRows.
 constexpr int kFusedCeMaxRows = 2048;
 
-__global__ void __launch_bounds__(32) k_ce_batch_sum(const float* row_loss, float* loss, int64_t rows, float lscale) {
-  vkc::pdl_wait();
-  vkc::pdl_trigger();
+__device__ __forceinline__ void ce_batch_sum_warp(const float* row_loss, float* loss, int64_t rows, float lscale) {
   const int lane = threadIdx.x & 31;
   Acc<VKC_SUM, true> acc;
   acc.init();
   if (rows <= 16) {
     if (lane == 0) {
-      for (int64_t k = 0; k < rows; ++k) acc.push(row_loss[k]);
+      for (int64_t k = 0; k < rows; ++k) acc.push(__ldcg(row_loss + k));
       loss[0] = acc.value() * lscale;
     }
     return;
   }
-  for (int64_t k = lane; k < rows; k += 32) acc.push(row_loss[k]);
+  for (int64_t k = lane; k < rows; k += 32) acc.push(__ldcg(row_loss + k));
   warp_reduce(acc);
   float v = __shfl_sync(0xffffffffu, acc.value(), 0);
   v *= lscale;
   if (lane == 0) loss[0] = v;
+}
+
+// k_cross_entropy and then the batch sum in the same launch: every block
+// stores its rows' losses and counts itself in `done`; the block that comes
+// last (it sees every other block's stores) runs the batch sum on its first
+// warp and puts `done` back to zero for the next launch.
+__global__ void __launch_bounds__(kThreads)
+k_cross_entropy_total(const float* x, const float* y, float* loss_rows, float* p_out, float* dx, int64_t rows,
+                      int64_t cols, float gscale, float* loss, float lscale, uint32_t* done) {
+  __shared__ uint32_t last;
+  vkc::pdl_wait();
+  vkc::pdl_trigger();
+  const int lane = threadIdx.x & 31;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r < rows) {
+    const float L = ce_row(x + r * cols, y + r * cols, p_out + r * cols, dx + r * cols, cols, 1, gscale);
+    if (lane == 0) loss_rows[r] = L;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < 32) ce_batch_sum_warp(loss_rows, loss, rows, lscale);
+  if (threadIdx.x == 0) *done = 0u;
 }
 
 // The reference's Adam chain (optimizers.py:235-253), one element per step:
@@ -458,6 +527,20 @@ VKC_EXPORT int vkc_dense_backward_ex(vkc_device_t dev, int precision, const floa
   return dense_backward_gemms(dev, precision, x, w, dy_act, dx, dw, db, batch, in_dim, out_dim, accumulate);
 }
 
+VKC_EXPORT int vkc_dense_backward_chain(vkc_device_t dev, int precision, const float* x, const float* w,
+                                        const float* dy, const float* dx_y, int dx_act, float* dx, float* dw,
+                                        float* db, int64_t batch, int64_t in_dim, int64_t out_dim, int accumulate) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(batch >= 0 && in_dim >= 0 && out_dim >= 0, "negative size");
+  VKC_REQUIRE(dx_act == VKC_ACT_NONE || dx_act == VKC_ACT_RELU || dx_act == VKC_ACT_SIGMOID,
+              "activation %d has no backward kernel", dx_act);
+  if (batch == 0) return VKC_OK;
+  VKC_REQUIRE(x && w && dy, "NULL buffer");
+  VKC_REQUIRE(dx_act == VKC_ACT_NONE || (dx && dx_y), "dx and its activation output are needed");
+  return dense_backward_gemms(dev, precision, x, w, dy, dx, dw, db, batch, in_dim, out_dim, accumulate, dx_y,
+                              dx_act);
+}
+
 VKC_EXPORT int vkc_softmax(vkc_device_t dev, const float* x, float* y, int64_t rows, int64_t cols) {
   VKC_BIND(dev);
   if (rows <= 0 || cols <= 0) return VKC_OK;
@@ -488,15 +571,10 @@ VKC_EXPORT int vkc_softmax_ce_fused(vkc_device_t dev, const float* x, const floa
   int r = vkc::scratch_alloc(dev, sizeof(float) * (size_t)rows, (void**)&row_loss);
   if (r != VKC_OK) return r;
   const unsigned grid = (unsigned)((rows * 32 + kThreads - 1) / kThreads);
-  cudaError_t e = vkc::launch_pdl(k_cross_entropy, dim3(grid), dim3(kThreads), 0, dev->stream, x, y, row_loss, p_out,
-                                  dx, rows, cols, 1, grad_scale);
-  r = e == cudaSuccess ? vkc::check_launch("softmax_ce_fused rows")
+  cudaError_t e = vkc::launch_pdl(k_cross_entropy_total, dim3(grid), dim3(kThreads), 0, dev->stream, x, y, row_loss,
+                                  p_out, dx, rows, cols, grad_scale, loss, loss_scale, dev->done_ctr);
+  r = e == cudaSuccess ? vkc::check_launch("softmax_ce_fused")
                        : vkc::set_error(VKC_ERR_CUDA, "softmax_ce_fused launch: %s", cudaGetErrorString(e));
-  if (r == VKC_OK) {
-    e = vkc::launch_pdl(k_ce_batch_sum, dim3(1), dim3(32), 0, dev->stream, row_loss, loss, rows, loss_scale);
-    r = e == cudaSuccess ? vkc::check_launch("softmax_ce_fused batch sum")
-                         : vkc::set_error(VKC_ERR_CUDA, "softmax_ce_fused launch: %s", cudaGetErrorString(e));
-  }
   vkc::scratch_free(dev, row_loss);
   return r;
 }

@@ -14,6 +14,7 @@ namespace vkc {
 
 std::atomic<uint64_t> g_launches{0};
 std::atomic<int> g_pdl{1};
+std::atomic<int> g_cluster_splitk{1};
 std::atomic<uint64_t> g_allocs{0};          // device + pinned host allocations requested
 std::atomic<int64_t> g_fail_alloc_in{-1};   // injected failure: fail when this reaches 0
 static thread_local std::string g_last_error;
@@ -161,8 +162,12 @@ VKC_EXPORT int vkc_device_open(int index, float priority, vkc_device_t* out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->side_stream, cudaStreamNonBlocking, prio);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->side_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->side_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&dev->bias_stream, cudaStreamNonBlocking, prio);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&dev->bias_join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&dev->err_word, sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemset(dev->err_word, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&dev->done_ctr, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(dev->done_ctr, 0, sizeof(uint32_t));
   if (e != cudaSuccess) {
     delete dev;
     return set_error(VKC_ERR_CUDA, "device setup: %s", cudaGetErrorString(e));
@@ -189,23 +194,29 @@ VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
   cudaStreamSynchronize(dev->copy_stream);
   cudaStreamSynchronize(dev->d2h_stream);
   if (dev->err_word) cudaFree(dev->err_word);
+  if (dev->done_ctr) cudaFree(dev->done_ctr);
   if (dev->xo_jump_pows) cudaFree(dev->xo_jump_pows);
   if (dev->xo_next_pows) cudaFree(dev->xo_next_pows);
   cudaStreamSynchronize(dev->side_stream);
+  cudaStreamSynchronize(dev->bias_stream);
   cudaEventDestroy(dev->copy_done);
   cudaEventDestroy(dev->d2h_after);
   cudaStreamDestroy(dev->d2h_stream);
   cudaEventDestroy(dev->side_fork);
   cudaEventDestroy(dev->side_join);
+  cudaEventDestroy(dev->bias_join);
   cudaStreamDestroy(dev->own_stream);
   cudaStreamDestroy(dev->copy_stream);
   cudaStreamDestroy(dev->side_stream);
+  cudaStreamDestroy(dev->bias_stream);
   delete dev;
   return VKC_OK;
 }
 
 VKC_EXPORT int vkc_device_synchronize(vkc_device_t dev) {
   VKC_BIND(dev);
+  VKC_CUDA(cudaStreamSynchronize(dev->side_stream));
+  VKC_CUDA(cudaStreamSynchronize(dev->bias_stream));
   VKC_CUDA(cudaStreamSynchronize(dev->copy_stream));
   VKC_CUDA(cudaStreamSynchronize(dev->d2h_stream));
   VKC_CUDA(cudaStreamSynchronize(dev->stream));
@@ -480,6 +491,27 @@ VKC_EXPORT int vkc_launch_count(uint64_t* count) {
 
 VKC_EXPORT int vkc_set_pdl(int enable) {
   vkc::g_pdl.store(enable ? 1 : 0, std::memory_order_relaxed);
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_side_defer(vkc_device_t dev, int defer) {
+  VKC_BIND(dev);
+  if (defer) {
+    dev->side_defer = 1;
+    return VKC_OK;
+  }
+  dev->side_defer = 0;
+  if (!dev->side_pending) return VKC_OK;
+  dev->side_pending = 0;
+  VKC_CUDA(cudaEventRecord(dev->side_join, dev->side_stream));
+  VKC_CUDA(cudaEventRecord(dev->bias_join, dev->bias_stream));
+  VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->side_join, 0));
+  VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->bias_join, 0));
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_set_cluster_splitk(int enable) {
+  vkc::g_cluster_splitk.store(enable ? 1 : 0, std::memory_order_relaxed);
   return VKC_OK;
 }
 

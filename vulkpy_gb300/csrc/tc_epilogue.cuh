@@ -17,18 +17,19 @@ namespace {
 constexpr uint32_t kEpiStageBytes = 32 * 32 * 4;  // per epilogue warp
 
 __device__ __forceinline__ float epi_value(float a, float alpha, float beta, float c, bool has_bias, float b, int act,
-                                           bool has_mask, float m) {
+                                           bool has_mask, float m, int mact = VKC_ACT_RELU) {
   float v = alpha * a;
   if (beta != 0.f) v += beta * c;
   if (has_bias) v += b;
   if (act == VKC_ACT_RELU) v = fmaxf(v, 0.f);
   else if (act == VKC_ACT_SIGMOID) v = 1.0f / (1.0f + expf(0.0f - v));
-  if (has_mask) v = relu_mask(v, m);
+  if (has_mask) v = act_deriv(v, m, mact);
   return v;
 }
 
 // The common epilogues in fixed form: alpha == 1, beta == 0, act none or
-// ReLU, v = a (+ bias) (max 0) (* ReLU'(mask)).  With alpha == 1 the product
+// ReLU, v = a (+ bias) (max 0) (* act'(mask), mact: ReLU or sigmoid).  With
+// alpha == 1 the product
 // alpha * a is exact, so these give epi_value's results bit for bit whatever
 // the compiler contracts.  get(j) is this lane's value of row j; the lane
 // writes column `col` of rows row0 .. row0+rows-1 (rows <= 32) through a
@@ -47,7 +48,7 @@ __device__ __forceinline__ float epi_value(float a, float alpha, float beta, flo
 // pointer to them would not fit the registers for 32).
 template <int NR, bool HB, bool RELU, bool HM, bool UPD, typename Get>
 __device__ __forceinline__ void epi_rows_fixed(Get get, float* C, const float* aux, float b, int64_t ld,
-                                               int64_t row0, int col, int rows) {
+                                               int64_t row0, int col, int rows, int mact = VKC_ACT_RELU) {
   float* cp = C + row0 * ld + col;
   float m[NR];
   if (HM || UPD) {
@@ -65,7 +66,7 @@ __device__ __forceinline__ void epi_rows_fixed(Get get, float* C, const float* a
       float v = get(j);
       if (HB) v = v + b;
       if (RELU) v = fmaxf(v, 0.f);
-      if (HM) v = relu_mask(v, m[j]);
+      if (HM) v = act_deriv(v, m[j], mact);
       *cp = v;
       if (UPD) *up = __fadd_rn(m[j], __fmul_rn(b, v));
     }
@@ -80,7 +81,7 @@ template <typename Get>
 __device__ __forceinline__ bool epi_rows_dispatch(Get get, float* C, const float* mask, float b, int64_t ld,
                                                   int64_t row0, int col, int rows, float alpha, float beta, int act,
                                                   bool hb, bool hm, bool raw, float* upd = nullptr,
-                                                  float upd_scale = 0.f) {
+                                                  float upd_scale = 0.f, int mact = VKC_ACT_RELU) {
   if (raw) {
     epi_rows_fixed<32, false, false, false, false>(get, C, nullptr, 0.f, ld, row0, col, rows);
     return true;
@@ -103,7 +104,7 @@ __device__ __forceinline__ bool epi_rows_dispatch(Get get, float* C, const float
     return true;
   }
   if (!hb && !relu) {
-    epi_rows_fixed<32, false, false, true, false>(get, C, mask, 0.f, ld, row0, col, rows);
+    epi_rows_fixed<32, false, false, true, false>(get, C, mask, 0.f, ld, row0, col, rows, mact);
     return true;
   }
   return false;
@@ -118,7 +119,8 @@ template <bool FIXED = true>
 __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float* __restrict__ stage, float* C,
                                                 const float* mask, const float* __restrict__ bias, int64_t ld,
                                                 int row0, int M, int col0, int N, float alpha, float beta, int act,
-                                                bool raw, float* upd = nullptr, float upd_scale = 0.f) {
+                                                bool raw, float* upd = nullptr, float upd_scale = 0.f,
+                                                int mact = VKC_ACT_RELU) {
   const int lane = threadIdx.x & 31;
   float4* srow = reinterpret_cast<float4*>(stage) + lane * 8;
 #pragma unroll
@@ -139,7 +141,8 @@ __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float
     return FIXED ? stage[j * 32 + so[j & 7]] : stage[j * 32 + ((((lane >> 2) ^ j) & 7) << 2) + (lane & 3)];
   };
   if (FIXED && cin &&
-      epi_rows_dispatch(staged, C, mask, b, ld, row0, col, rows, alpha, beta, act, hb, hm, raw, upd, upd_scale)) {
+      epi_rows_dispatch(staged, C, mask, b, ld, row0, col, rows, alpha, beta, act, hb, hm, raw, upd, upd_scale,
+                        mact)) {
   } else if (cin) {
 #pragma unroll 1
     for (int j0 = 0; j0 < rows; j0 += 16) {
@@ -157,7 +160,8 @@ __device__ __forceinline__ void epilogue_tile32(const uint32_t (&acc)[32], float
       for (int t = 0; t < 16; ++t) {
         if (j0 + t < rows) {
           const float a = staged(j0 + t);
-          C[(int64_t)(row0 + j0 + t) * ld + col] = raw ? a : epi_value(a, alpha, beta, cv[t], hb, b, act, hm, mv[t]);
+          C[(int64_t)(row0 + j0 + t) * ld + col] =
+              raw ? a : epi_value(a, alpha, beta, cv[t], hb, b, act, hm, mv[t], mact);
         }
       }
     }

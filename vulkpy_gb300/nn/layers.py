@@ -96,12 +96,37 @@ class Dense(Module):
             wg._dptr() if wg is not None else None, bg._dptr() if bg is not None else None,
             dy_act.shape[0], self.input_dim, self.output_dim, 1 if accumulate else 0))
         dy._written()
+        # held until the next call: a weight GEMM on a branch stream may still
+        # read it after this returns (the caller may defer the join)
+        self._act_dy = dy
         if wg is not None:
             wg._written()
         if bg is not None:
             bg._written()
         if dx is not None:
             dx._written()
+        return dx
+
+    def backward_chain(self, dy: Array, act: int, y: Array, accumulate: bool = True) -> Array:
+        """This layer's backward followed by the backward of the activation
+        below it (output ``y``): returns ``(dy W) * act'(y)``, the gradient
+        the Dense layer under that activation receives, with the derivative
+        applied inside the input-gradient GEMM; the same float32 results as
+        ``backward`` then the activation's backward."""
+        x = self._x
+        gpu = dy._gpu
+        dx = Array(gpu, shape=(dy.shape[0], self.input_dim))
+        wg = self.w.grad
+        bg = self.b.grad
+        check(lib.vkc_dense_backward_chain(
+            dy._h, _PREC[gpu.matmul_precision], x._dptr(), self.w.value._dptr(), dy._dptr(), y._dptr(), act,
+            dx._buf.ptr or 0, wg._dptr() if wg is not None else None, bg._dptr() if bg is not None else None,
+            dy.shape[0], self.input_dim, self.output_dim, 1 if accumulate else 0))
+        if wg is not None:
+            wg._written()
+        if bg is not None:
+            bg._written()
+        dx._written()
         return dx
 
     def zero_grad(self):

@@ -62,15 +62,40 @@ class Sequence:
         layers overwrite their gradients (each is written once per step)
         instead of adding to them."""
         dx = self.loss.grad()
+        # the Dense layers' weight GEMMs and bias sums stay on branch streams
+        # until the whole backward is issued (joined back in the finally)
+        # The gradients passed down are kept alive until then: a buffer freed
+        # (stream-ordered, on the device's stream) while a branch still reads
+        # it could be handed to the next allocation.
+        h = dx._h
+        keep = [dx]
+        check(lib.vkc_side_defer(h, 1))
+        try:
+            self._backward_layers(dx, accumulate, keep)
+        finally:
+            check(lib.vkc_side_defer(h, 0))
+            del keep
+
+    def _backward_layers(self, dx, accumulate: bool, keep: list):
         k = len(self.L) - 1
         while k >= 0:
             layer = self.L[k]
             prev = self.L[k - 1] if k >= 1 else None
+            below = self.L[k - 2] if k >= 2 else None
+            if (self.fuse and type(layer) is Dense and type(prev) in (ReLU, Sigmoid) and type(below) is Dense
+                    and getattr(prev, "_y", None) is not None and len(dx.shape) == 2):
+                # this layer's backward with the activation's below it in the
+                # same GEMM: dx is already the lower Dense layer's dy
+                dx = layer.backward_chain(dx, prev.act, prev._y, accumulate=accumulate)
+                keep.append(dx)
+                k -= 2
+                continue
             if (self.fuse and type(layer) in (ReLU, Sigmoid) and type(prev) is Dense
                     and getattr(layer, "_y", None) is not None
                     and len(dx.shape) == 2):
                 # the activation's backward and the Dense bias sum in one kernel
                 dx = prev.backward_act(dx, layer.act, layer._y, need_dx=k - 1 > 0, accumulate=accumulate)
+                keep.append(dx)
                 k -= 2
                 continue
             if type(layer) is Dense:
@@ -79,6 +104,7 @@ class Sequence:
                 layer.backward(dx, need_dx=False)
             else:
                 dx = layer.backward(dx)
+            keep.append(dx)
             k -= 1
 
     def _overwrites_grads(self) -> bool:
