@@ -1013,7 +1013,7 @@ def main():
     ap.add_argument("--n-idx", type=int, default=N_IDX)
     ap.add_argument("--states", type=int, default=PRNG_STATES)
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-rows", type=int, default=256)
+    ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--cpu-passes", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the matmul and MLP studies")
