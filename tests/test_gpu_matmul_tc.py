@@ -170,7 +170,7 @@ def test_cluster_splitk_matches_reduction_launch(gpu, vk, m, n, k, prec):
                     if args == (1.0, 0.0, False, 0):
                         assert rel_fro(got, exp) < (1e-5 if prec == "bf16x3" else 8e-3)
     finally:
-        _lib.lib.vkc_set_cluster_splitk(1)
+        _lib.lib.vkc_set_cluster_splitk(0)   # the default
         _lib.lib.vkc_gemm_tune_set(P, m, n, k, 0)
         autotune.load_table()
     assert gpu.check_errors() == 0

@@ -303,7 +303,7 @@ def test_backward_chain_matches_backward_then_activation(gpu, vk, prec, B, I, Ou
                     np.testing.assert_array_equal(gb, np.asarray(d.b.grad))
     finally:
         gpu.matmul_precision = old
-        _lib.lib.vkc_set_cluster_splitk(1)
+        _lib.lib.vkc_set_cluster_splitk(0)   # the default
         _lib.lib.vkc_gemm_tune_set(P, B, I, Out, 0)
         autotune.load_table()
     assert gpu.check_errors() == 0

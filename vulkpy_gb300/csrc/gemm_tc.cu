@@ -796,10 +796,12 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
   // 2..8 K ranges: the ranges of a tile run as one cluster and reduce in the
   // kernel (units u = tile * splits + z go to CTA u mod grid, and a grid of
   // whole clusters gives the CTAs of a cluster the splits of one tile).
-  // Only outside a stream capture: it saves a launch's host cost (MLP step
-  // eager 6.1k -> 6.4k steps/s), but in a CUDA graph the separate reduction,
-  // overlapped with the GEMM's tail by programmatic dependent launch, is
-  // faster (10.4k against 8.7k steps/s with the cluster form).
+  // Only when switched on (vkc_set_cluster_splitk) and outside a stream
+  // capture: it saves a launch's host cost (MLP step eager 6.1k -> 6.4k
+  // steps/s) but costs device time -- in a CUDA graph the separate
+  // reduction, overlapped with the GEMM's tail by programmatic dependent
+  // launch, is faster (10.4k against 8.7k steps/s), and so is an eager
+  // 1024^3 bf16 product (0.022 against 0.026 ms).
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(dev->stream, &cap) != cudaSuccess) {
     cudaGetLastError();

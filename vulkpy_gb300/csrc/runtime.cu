@@ -14,7 +14,7 @@ namespace vkc {
 
 std::atomic<uint64_t> g_launches{0};
 std::atomic<int> g_pdl{1};
-std::atomic<int> g_cluster_splitk{1};
+std::atomic<int> g_cluster_splitk{0};
 std::atomic<uint64_t> g_allocs{0};          // device + pinned host allocations requested
 std::atomic<int64_t> g_fail_alloc_in{-1};   // injected failure: fail when this reaches 0
 static thread_local std::string g_last_error;
