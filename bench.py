@@ -359,7 +359,10 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
             pending = cur
         collect(pending)
 
-    run(max(1, args.warmup))
+    # a few more untimed steps than the kernel leg: the first pipelined steps
+    # still fill the device's cache of upload buffers (one 1 GiB and one
+    # 256 MiB allocation show up as multi-millisecond host stalls)
+    run(max(1, args.warmup) + 3)
     gpu.wait()
     if dist is not None:
         dist.barrier()
@@ -1012,7 +1015,7 @@ def main():
     ap.add_argument("--cols", type=int, default=COLS)
     ap.add_argument("--n-idx", type=int, default=N_IDX)
     ap.add_argument("--states", type=int, default=PRNG_STATES)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--cpu-passes", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")

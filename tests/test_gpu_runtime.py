@@ -278,3 +278,48 @@ def test_pipelined_steps_match_serial(gpu, vk):
     for a, b in zip(serial, got):
         for u, v in zip(a, b):
             np.testing.assert_array_equal(u, v)
+
+
+def test_upload_buffers_are_reused_after_their_last_use(gpu, vk):
+    """A freed upload buffer (>= 1 MiB) is cached with an event after its
+    last use on the compute stream; an upload of the same size takes it
+    without allocating once that use has finished, and allocates instead
+    while it is still queued.  Results of ops queued on old contents stay
+    correct either way."""
+    from vulkpy_gb300 import _lib
+    rng = np.random.default_rng(11)
+    n = 1 << 22                                   # 16 MiB of float32
+    hosts = [rng.standard_normal(n).astype(np.float32) for _ in range(6)]
+    pins = []
+    for h in hosts:
+        p_ = vk.vkarray.empty_pinned(h.shape)
+        p_[...] = h
+        pins.append(p_)
+
+    def allocs():
+        c = C.c_uint64()
+        assert _lib.lib.vkc_alloc_count(C.byref(c)) == 0
+        return c.value
+
+    outs = []
+    a = vk.Array(gpu, data=pins[0])
+    for i in range(1, 6):
+        y = a
+        for _ in range(8):                        # queue work that reads the buffer
+            y = y * 1.5 + 1.0
+        outs.append(y)
+        del a, y
+        if i % 2:
+            gpu.wait()                            # the last use has finished: reused
+            before = allocs()
+            a = vk.Array(gpu, data=pins[i])
+            assert allocs() == before, "a finished cached upload buffer should have been reused"
+        else:
+            a = vk.Array(gpu, data=pins[i])       # maybe still queued: either way correct
+    outs.append(a * 1.0)
+    for i, o in enumerate(outs[:5]):
+        exp = hosts[i].astype(np.float32)
+        for _ in range(8):
+            exp = exp * np.float32(1.5) + np.float32(1.0)
+        np.testing.assert_array_equal(np.asarray(o), exp)
+    np.testing.assert_array_equal(np.asarray(outs[5]), hosts[5])

@@ -10,6 +10,8 @@
 #include <mutex>
 #include <string>
 #include <utility>
+#include <unordered_map>
+#include <vector>
 
 #include "../../include/vulkpy_gb300.h"
 
@@ -22,6 +24,17 @@ struct vkc_device {
   cudaStream_t own_stream = nullptr;   // compute stream created at open
   cudaStream_t stream = nullptr;       // current compute stream (own or user's)
   cudaStream_t copy_stream = nullptr;  // uploads into fresh buffers
+  cudaMemPool_t upload_pool = nullptr; // their buffers (reused only by later uploads)
+  // Upload buffers the caller freed, each with an event on the compute stream
+  // after its last use: the next upload of the same size takes one (waiting
+  // on that event if needed) instead of allocating (vkc_free / vkc_upload*).
+  struct UploadBlock {
+    void* ptr;
+    size_t bytes;
+    cudaEvent_t freed;
+  };
+  std::vector<UploadBlock> upload_free;
+  std::unordered_map<void*, size_t> upload_live;  // upload buffers in use, by size
   cudaEvent_t copy_done = nullptr;     // reused marker for uploads
   cudaStream_t d2h_stream = nullptr;   // asynchronous read-backs (vkc_d2h_async)
   cudaEvent_t d2h_after = nullptr;     // reused marker: compute work a read-back follows

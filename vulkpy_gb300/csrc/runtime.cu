@@ -181,6 +181,28 @@ VKC_EXPORT int vkc_device_open(int index, float priority, vkc_device_t* out) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
+  // Uploads get their own pool.  Their buffers are allocated on the copy
+  // stream and freed on the compute stream; in the shared pool the compute
+  // stream's own allocations took the freed blocks first, so an upload
+  // issued while compute runs often found no finished free block and the
+  // pool grew (milliseconds of host time) or the copy waited on compute.
+  // Here an upload reuses an earlier upload's block once its free has
+  // completed, and never waits on the compute stream for one.
+  {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = index;
+    if (cudaMemPoolCreate(&dev->upload_pool, &props) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      int no = 0;
+      cudaMemPoolSetAttribute(dev->upload_pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      cudaMemPoolSetAttribute(dev->upload_pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+    } else {
+      dev->upload_pool = nullptr;
+    }
+  }
   cudaGetLastError();
   *out = dev;
   return VKC_OK;
@@ -193,6 +215,12 @@ VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
   if (dev->stream != dev->own_stream) cudaStreamSynchronize(dev->stream);
   cudaStreamSynchronize(dev->copy_stream);
   cudaStreamSynchronize(dev->d2h_stream);
+  for (auto& b : dev->upload_free) {
+    cudaFreeAsync(b.ptr, dev->own_stream);
+    cudaEventDestroy(b.freed);
+  }
+  dev->upload_free.clear();
+  cudaStreamSynchronize(dev->own_stream);
   if (dev->err_word) cudaFree(dev->err_word);
   if (dev->done_ctr) cudaFree(dev->done_ctr);
   if (dev->xo_jump_pows) cudaFree(dev->xo_jump_pows);
@@ -209,6 +237,8 @@ VKC_EXPORT int vkc_device_close(vkc_device_t dev) {
   cudaStreamDestroy(dev->copy_stream);
   cudaStreamDestroy(dev->side_stream);
   cudaStreamDestroy(dev->bias_stream);
+  // released once its last buffer is freed
+  if (dev->upload_pool) cudaMemPoolDestroy(dev->upload_pool);
   delete dev;
   return VKC_OK;
 }
@@ -261,9 +291,72 @@ VKC_EXPORT int vkc_alloc(vkc_device_t dev, size_t bytes, void** ptr) {
   return scratch_alloc(dev, bytes, ptr);
 }
 
+namespace {
+constexpr size_t kUploadCacheBlocks = 8;          // cached upload buffers per device at most
+constexpr size_t kUploadCacheMin = size_t(1) << 20;  // smaller uploads allocate every time
+
+// A device buffer of `bytes` for an upload on the copy stream (dev->mu
+// held): a cached buffer of that size whose last use has finished, else a
+// new allocation from the upload pool.  A cached buffer whose last use is
+// still queued is not waited for: its free event is recorded when the
+// caller drops the array, after everything then queued on the compute
+// stream, so waiting would hold the copy behind the current compute (in a
+// pipelined loop, the buffer freed two steps back is the finished one).
+int upload_take(vkc_device_t dev, size_t bytes, void** p) {
+  const bool cached = bytes >= kUploadCacheMin;
+  for (size_t i = 0; cached && i < dev->upload_free.size(); ++i) {
+    if (dev->upload_free[i].bytes != bytes) continue;
+    if (cudaEventQuery(dev->upload_free[i].freed) != cudaSuccess) continue;
+    vkc_device::UploadBlock b = dev->upload_free[i];
+    dev->upload_free.erase(dev->upload_free.begin() + (long)i);
+    cudaEventDestroy(b.freed);
+    *p = b.ptr;
+    dev->upload_live[b.ptr] = bytes;
+    return VKC_OK;
+  }
+  cudaGetLastError();  // a not-ready query is not an error
+  if (vkc::alloc_should_fail())
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): injected allocation failure", bytes);
+  cudaError_t e = dev->upload_pool ? cudaMallocFromPoolAsync(p, bytes, dev->upload_pool, dev->copy_stream)
+                                   : cudaMallocAsync(p, bytes, dev->copy_stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  if (cached) dev->upload_live[*p] = bytes;
+  return VKC_OK;
+}
+}  // namespace
+
 VKC_EXPORT int vkc_free(vkc_device_t dev, void* ptr) {
   if (!ptr) return VKC_OK;
   VKC_BIND(dev);
+  {
+    // a large upload buffer goes to the device's upload cache with an event
+    // after its last use on the compute stream (see upload_take)
+    std::lock_guard<std::mutex> lk(dev->mu);
+    auto it = dev->upload_live.find(ptr);
+    if (it != dev->upload_live.end()) {
+      const size_t bytes = it->second;
+      dev->upload_live.erase(it);
+      cudaEvent_t ev = nullptr;
+      if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess &&
+          cudaEventRecord(ev, dev->stream) == cudaSuccess) {
+        if (dev->upload_free.size() >= kUploadCacheBlocks) {
+          // the oldest cached buffer goes back to its pool, after its last use
+          VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->upload_free.front().freed, 0));
+          VKC_CUDA(cudaFreeAsync(dev->upload_free.front().ptr, dev->stream));
+          cudaEventDestroy(dev->upload_free.front().freed);
+          dev->upload_free.erase(dev->upload_free.begin());
+        }
+        dev->upload_free.push_back({ptr, bytes, ev});
+        return VKC_OK;
+      }
+      if (ev) cudaEventDestroy(ev);
+      cudaGetLastError();
+    }
+  }
   VKC_CUDA(cudaFreeAsync(ptr, dev->stream));
   return VKC_OK;
 }
@@ -289,6 +382,7 @@ VKC_EXPORT int vkc_host_free(void* ptr) {
   return VKC_OK;
 }
 
+
 VKC_EXPORT int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void** dptr) {
   VKC_BIND(dev);
   VKC_REQUIRE(dptr && (src || bytes == 0), "NULL argument");
@@ -298,16 +392,10 @@ VKC_EXPORT int vkc_upload(vkc_device_t dev, const void* src, size_t bytes, void*
   VKC_CUDA(cudaStreamIsCapturing(dev->stream, &cap));
   VKC_REQUIRE(cap == cudaStreamCaptureStatusNone, "host uploads are not allowed while the stream is captured");
   std::lock_guard<std::mutex> lk(dev->mu);
-  if (vkc::alloc_should_fail())
-    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): injected allocation failure", bytes);
   // Allocate and copy on the copy stream so that the upload does not queue
   // behind compute work; the compute stream then waits for the copy.
-  cudaError_t e = cudaMallocAsync(dptr, bytes, dev->copy_stream);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    *dptr = nullptr;
-    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
-  }
+  const int r = upload_take(dev, bytes, dptr);
+  if (r != VKC_OK) return r;
   VKC_CUDA(cudaMemcpyAsync(*dptr, src, bytes, cudaMemcpyHostToDevice, dev->copy_stream));
   VKC_CUDA(cudaEventRecord(dev->copy_done, dev->copy_stream));
   VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->copy_done, 0));
@@ -343,14 +431,8 @@ VKC_EXPORT int vkc_upload_async(vkc_device_t dev, const void* src, size_t bytes,
   VKC_CUDA(cudaStreamIsCapturing(dev->stream, &cap));
   VKC_REQUIRE(cap == cudaStreamCaptureStatusNone, "host uploads are not allowed while the stream is captured");
   std::lock_guard<std::mutex> lk(dev->mu);
-  if (vkc::alloc_should_fail())
-    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): injected allocation failure", bytes);
-  cudaError_t e = cudaMallocAsync(dptr, bytes, dev->copy_stream);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    *dptr = nullptr;
-    return set_error(VKC_ERR_OOM, "cudaMallocAsync(%zu bytes): %s", bytes, cudaGetErrorString(e));
-  }
+  const int r = upload_take(dev, bytes, dptr);
+  if (r != VKC_OK) return r;
   VKC_CUDA(cudaMemcpyAsync(*dptr, src, bytes, cudaMemcpyHostToDevice, dev->copy_stream));
   VKC_CUDA(cudaEventRecord(dev->copy_done, dev->copy_stream));
   VKC_CUDA(cudaStreamWaitEvent(dev->stream, dev->copy_done, 0));
