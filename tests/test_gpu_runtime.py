@@ -323,3 +323,30 @@ def test_upload_buffers_are_reused_after_their_last_use(gpu, vk):
             exp = exp * np.float32(1.5) + np.float32(1.0)
         np.testing.assert_array_equal(np.asarray(o), exp)
     np.testing.assert_array_equal(np.asarray(outs[5]), hosts[5])
+
+
+def test_whole_array_assignment_uploads_in_place(gpu, vk):
+    """a[:] = host array (pageable or pinned, same shape) overwrites the
+    device buffer with one copy ordered after the ops already queued on it:
+    those see the old contents, later ops the new; no read-back happens."""
+    rng = np.random.default_rng(3)
+    x, y, z = (rng.standard_normal((512, 300)).astype(np.float32) for _ in range(3))
+    a = vk.Array(gpu, data=x)
+    b = a * 2.0                         # queued on the old contents
+    a[:] = y                            # pageable
+    c = a + 1.0
+    zp = vk.vkarray.empty_pinned(z.shape)
+    zp[...] = z
+    a.prefetch()                        # a read-back in flight before the next overwrite
+    a[...] = zp                         # pinned
+    d = a * 3.0
+    np.testing.assert_array_equal(np.asarray(b), x * np.float32(2.0))
+    np.testing.assert_array_equal(np.asarray(c), y + np.float32(1.0))
+    np.testing.assert_array_equal(np.asarray(d), z * np.float32(3.0))
+    np.testing.assert_array_equal(np.asarray(a), z)
+    a[:] = x.astype(np.float64)         # converted to float32 first
+    np.testing.assert_array_equal(np.asarray(a), x)
+    a[:, 0] = 5.0                       # partial writes still go through the host mirror
+    exp = x.copy()
+    exp[:, 0] = 5.0
+    np.testing.assert_array_equal(np.asarray(a * 1.0), exp)

@@ -627,6 +627,11 @@ struct AdamItem {
   int64_t n;
   int block0, chunks;
 };
+// Adam chunks: 1024 elements (one float4 of each array per thread), so a
+// step's ~2M parameters make several blocks per SM whose loads and stores
+// overlap (4096-element chunks made one wave of ~3 blocks per SM that all
+// loaded, then all computed, then all stored).
+constexpr int kAdamChunk = 1024;
 struct AdamTable {
   int count, total;
   float b1, c1, b2, c2, eps, nlr;
@@ -660,17 +665,18 @@ __global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ Ad
     const AdamItem& I = tab.it[lo];
     const double p1 = I.powers[0] * tab.beta1, p2 = I.powers[1] * tab.beta2;
     const float d1 = (float)(1.0 - p1), d2 = (float)(1.0 - p2);
-    const int64_t i0 = (int64_t)(t - I.block0) * kVecChunk;
-    const int64_t i1 = min(i0 + kVecChunk, I.n);
+    const int64_t i0 = (int64_t)(t - I.block0) * kAdamChunk;
+    const int64_t i1 = min(i0 + kAdamChunk, I.n);
     const bool vec = ((reinterpret_cast<uintptr_t>(I.value) | reinterpret_cast<uintptr_t>(I.grad) |
                        reinterpret_cast<uintptr_t>(I.m) | reinterpret_cast<uintptr_t>(I.v)) & 15u) == 0;
-    if (vec && i1 - i0 == kVecChunk) {
-      // a full chunk: 4 float4 of each array per thread, every load issued
+    if (vec && i1 - i0 == kAdamChunk) {
+      // a full chunk: a float4 of each array per thread, every load issued
       // before the first store (the four arrays are distinct, but the
       // compiler cannot know it)
-      float4 gg[4], mm[4], vv[4], xx[4];
+      constexpr int kU = kAdamChunk / 1024;
+      float4 gg[kU], mm[kU], vv[kU], xx[kU];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < kU; ++u) {
         const int64_t i = i0 + (int64_t)(u * 256 + threadIdx.x) * 4;
         gg[u] = *reinterpret_cast<const float4*>(I.grad + i);
         mm[u] = *reinterpret_cast<const float4*>(I.m + i);
@@ -678,7 +684,7 @@ __global__ void __launch_bounds__(256) k_adam_grouped(const __grid_constant__ Ad
         xx[u] = *reinterpret_cast<const float4*>(I.value + i);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < kU; ++u) {
         const int64_t i = i0 + (int64_t)(u * 256 + threadIdx.x) * 4;
         adam_elem(tab, d1, d2, gg[u].x, mm[u].x, vv[u].x, xx[u].x);
         adam_elem(tab, d1, d2, gg[u].y, mm[u].y, vv[u].y, xx[u].y);
@@ -1167,7 +1173,7 @@ VKC_EXPORT int vkc_adam_update_grouped(vkc_device_t dev, float* const* value, co
       VKC_REQUIRE(powers[i] && (n[i] == 0 || (value[i] && grad[i] && m[i] && v[i])), "NULL buffer");
       AdamItem& I = tab.it[tab.count++];
       I = AdamItem{value[i], grad[i], m[i], v[i], powers[i], n[i], total,
-                   (int)std::max<int64_t>(1, (n[i] + kVecChunk - 1) / kVecChunk)};
+                   (int)std::max<int64_t>(1, (n[i] + kAdamChunk - 1) / kAdamChunk)};
       total += I.chunks;  // an empty tensor still gets one chunk: its powers advance
     }
     tab.total = total;

@@ -332,11 +332,22 @@ int upload_take(vkc_device_t dev, size_t bytes, void** p) {
 VKC_EXPORT int vkc_free(vkc_device_t dev, void* ptr) {
   if (!ptr) return VKC_OK;
   VKC_BIND(dev);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(dev->stream, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;
+  }
   {
     // a large upload buffer goes to the device's upload cache with an event
-    // after its last use on the compute stream (see upload_take)
+    // after its last use on the compute stream (see upload_take); not while
+    // the stream is captured (the event would be a graph node, recorded only
+    // when the graph runs), then it is freed like any buffer
     std::lock_guard<std::mutex> lk(dev->mu);
     auto it = dev->upload_live.find(ptr);
+    if (it != dev->upload_live.end() && cap != cudaStreamCaptureStatusNone) {
+      dev->upload_live.erase(it);
+      it = dev->upload_live.end();
+    }
     if (it != dev->upload_live.end()) {
       const size_t bytes = it->second;
       dev->upload_live.erase(it);

@@ -583,6 +583,25 @@ class _GPUArray(Resource):
                 check(lib.vkc_fill_u32(self._gpu._dev.h, self._buf.ptr or 0, self._size, int(value) & 0xFFFFFFFF))
             self._written()
             return
+        if (self._is_full(key) and isinstance(value, np.ndarray) and value.shape == self.shape and self._size
+                and self._gpu._dev.capture is None):
+            # whole-array overwrite from host memory: one copy on the device's
+            # stream, after the ops queued on the array -- no read-back of the
+            # old contents, no pass through the host mirror (a pinned source is
+            # read asynchronously and kept alive until its copy is done)
+            src = np.ascontiguousarray(value, dtype=self._dtype)
+            self._wait_d2h()   # a read-back in flight still reads the buffer
+            self._wait_h2d()   # and an upload in flight still reads its source
+            self._ensure_device_for_overwrite()
+            dev = self._gpu._dev
+            if _is_pinned(src):
+                j = C.c_void_p()
+                check(lib.vkc_h2d(dev.h, self._buf.ptr, src.ctypes.data, self._buf.nbytes, C.byref(j)))
+                self._h2d_job, self._h2d_src = j.value, src
+            else:
+                check(lib.vkc_h2d(dev.h, self._buf.ptr, src.ctypes.data, self._buf.nbytes, None))
+            self._written()
+            return
         h = self._ensure_host()
         self._wait_h2d()
         h[key] = value
