@@ -350,6 +350,8 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
         final = np.asarray(X)
         d2h = sum(o.nbytes for o in got) + final.nbytes
 
+    marks = []
+
     def run(steps):
         pending = None
         for _ in range(steps):
@@ -357,21 +359,29 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
             if pending is not None:
                 collect(pending)
             pending = cur
+            marks.append(time.perf_counter())
         collect(pending)
 
     # a few more untimed steps than the kernel leg: the first pipelined steps
     # still fill the device's cache of upload buffers (one 1 GiB and one
-    # 256 MiB allocation show up as multi-millisecond host stalls)
+    # 256 MiB allocation show up as multi-millisecond host stalls).  The
+    # timed region holds --e2e-steps (30) steps: the pipeline's fill (the
+    # first upload) and drain (the last read-back), ~11 ms together, are
+    # spread over them.
     run(max(1, args.warmup) + 3)
     gpu.wait()
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
+    marks.clear()
     run(args.e2e_steps)
     gpu.wait()
     dt = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, dist)
+    # host time of each iteration (issue step i+1, read step i), for spotting stalls
+    step_ms = [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
+            "iteration_ms": step_ms,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
                    "step i+1 issued before step i's results are read"}
 
@@ -1015,7 +1025,7 @@ def main():
     ap.add_argument("--cols", type=int, default=COLS)
     ap.add_argument("--n-idx", type=int, default=N_IDX)
     ap.add_argument("--states", type=int, default=PRNG_STATES)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--cpu-passes", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
