@@ -372,18 +372,25 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     gpu.wait()
     if dist is not None:
         dist.barrier()
-    t0 = time.perf_counter()
-    marks.clear()
-    run(args.e2e_steps)
-    gpu.wait()
-    dt = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, dist)
-    # host time of each iteration (issue step i+1, read step i), for spotting stalls
-    step_ms = [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]
+    # Three timed repetitions, the best reported (as for the CPU baseline):
+    # the host sometimes stalls for tens of milliseconds in one iteration
+    # (seen once in ~100 iterations, not reproducible in isolation).
+    reps = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        marks.clear()
+        run(args.e2e_steps)
+        gpu.wait()
+        dt_rep = (time.perf_counter() - t0) / args.e2e_steps
+        # host time of each iteration (issue step i+1, read step i), for spotting stalls
+        reps.append((dt_rep, [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]))
+    dt_best, step_ms = min(reps, key=lambda r: r[0])
+    dt = max_over_ranks(dt_best, dist)
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
-            "iteration_ms": step_ms,
+            "iteration_ms": step_ms, "repetitions_ms": [round(r[0] * 1e3, 3) for r in reps],
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
-                   "step i+1 issued before step i's results are read"}
+                   "step i+1 issued before step i's results are read; best of 3 timed repetitions"}
 
 
 # ---------------------------------------------------------------- matmul / MLP
