@@ -17,7 +17,9 @@ One step, in order (all through the vulkpy API):
   X op= row, X op= col for op in + - * /  (in place)         8 launches, 8 B/el
 metric = algorithmic bytes of the step / step time (GB/s).  Inputs stay in
 HBM for `value`; the `e2e` leg uploads X, row, col, idx from pinned host
-memory and reads the reduction results and the final X back every step.
+memory and reads the reduction results and the final X back every step
+(pipelined: step i's read-back and step i+1's upload overlap the compute;
+30 steps per timed repetition, best of three repetitions).
 """
 from __future__ import annotations
 
