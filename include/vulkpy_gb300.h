@@ -459,6 +459,18 @@ int vkc_xoshiro_randrange(vkc_device_t dev, uint32_t* state, uint32_t size, uint
 int vkc_dense_forward(vkc_device_t dev, int precision, const float* x, const float* w,
                       const float* bias, float* y, int64_t batch, int64_t in_dim,
                       int64_t out_dim, int act);
+/* A stack of Dense layers, y[l] = act[l](in_l W[l]^T + bias[l]) with in_0 = x
+ * and in_l = y[l-1], dims[0..layers] the widths (layer l: dims[l] ->
+ * dims[l+1]), the same results as vkc_dense_forward layer by layer bit for
+ * bit (models.py:40-53 runs the layers one after the other).  On the
+ * tensor-core path the operand pre-pass of layer l+1's input is written by
+ * layer l's split-K reduction (or one pre-pass launch when it has none), and
+ * the weights of layers 1.. are split on a side stream at the start: one
+ * launch fewer on the chain per layer after the first.  bias[l] may be
+ * NULL. */
+int vkc_dense_stack_forward(vkc_device_t dev, int precision, int layers, const float* x, int64_t batch,
+                            const int64_t* dims, const float* const* w, const float* const* bias,
+                            const int* act, float* const* y);
 /* Given dy (already multiplied by the activation derivative when act != NONE
  * is applied by the caller), accumulate dW += dy^T x, db += sum_b dy and write
  * dx = dy @ w (dx may be NULL).  nn/layers.py:104-141 without the (B,out,in)

@@ -307,3 +307,48 @@ def test_backward_chain_matches_backward_then_activation(gpu, vk, prec, B, I, Ou
         _lib.lib.vkc_gemm_tune_set(P, B, I, Out, 0)
         autotune.load_table()
     assert gpu.check_errors() == 0
+
+
+@pytest.mark.parametrize("prec", ["bf16", "bf16x3"])
+@pytest.mark.parametrize("dims,batch", [((784, 1024, 1024, 10), 256), ((100, 300, 130, 7), 37), ((64, 96, 64), 130)])
+def test_dense_stack_forward_matches_layer_by_layer(gpu, vk, prec, dims, batch):
+    """vkc_dense_stack_forward (each layer's split-K reduction writing the
+    next layer's operand pre-pass, weights split on a side stream) gives the
+    bits of vkc_dense_forward layer by layer, whole-K and split-K plans."""
+    import ctypes as C
+    from vulkpy_gb300 import _lib, autotune
+    P = {"bf16": _lib.MM_BF16, "bf16x3": _lib.MM_BF16X3}[prec]
+    rng = np.random.default_rng(sum(dims) + batch)
+    X = rng.standard_normal((batch, dims[0])).astype(f32)
+    Ws = [(rng.standard_normal((o, i)) / np.sqrt(i)).astype(f32) for i, o in zip(dims[:-1], dims[1:])]
+    bs = [rng.standard_normal(o).astype(f32) for o in dims[1:]]
+    acts = [_lib.ACT_RELU, _lib.ACT_SIGMOID, _lib.ACT_NONE][:len(Ws)]
+    acts[-1] = _lib.ACT_NONE
+    x = vk.Array(gpu, data=X)
+    w = [vk.Array(gpu, data=a) for a in Ws]
+    b = [vk.Array(gpu, data=a) for a in bs]
+    k = len(Ws)
+    try:
+        for splits in (0, 1, 3, 8):
+            if splits:
+                for i, o in zip(dims[:-1], dims[1:]):
+                    _lib.lib.vkc_gemm_plan_set(P, batch, o, i, splits, 128)
+            ys = [vk.Array(gpu, shape=(batch, o)) for o in dims[1:]]
+            ptrs = lambda v: (C.c_void_p * k)(*v)
+            st = _lib.lib.vkc_dense_stack_forward(
+                gpu.handle, P, k, x._dptr(), batch, (C.c_int64 * (k + 1))(*dims), ptrs([a._dptr() for a in w]),
+                ptrs([a._dptr() for a in b]), (C.c_int * k)(*acts), ptrs([y._buf.ptr for y in ys]))
+            assert st == 0, _lib.last_error()
+            inp = x
+            for l in range(k):
+                ys[l]._written()
+                ref = vk.Array(gpu, shape=(batch, dims[l + 1]))
+                assert _lib.lib.vkc_dense_forward(gpu.handle, P, inp._dptr(), w[l]._dptr(), b[l]._dptr(), ref._buf.ptr,
+                                                  batch, dims[l], dims[l + 1], acts[l]) == 0
+                ref._written()
+                np.testing.assert_array_equal(np.asarray(ys[l]), np.asarray(ref), err_msg=str((splits, l)))
+                inp = ys[l]
+    finally:
+        _lib.lib.vkc_gemm_tune_clear()
+        autotune.load_table()
+    assert gpu.check_errors() == 0

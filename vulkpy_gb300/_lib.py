@@ -132,6 +132,7 @@ _SIGS = {
     "vkc_box_muller": ([vp, vp, vp, sz, f32, f32], i32),
     "vkc_xoshiro_randrange": ([vp, vp, u32, vp, sz, u32, u32], i32),
     "vkc_dense_forward": ([vp, i32, vp, vp, vp, vp, i64, i64, i64, i32], i32),
+    "vkc_dense_stack_forward": ([vp, i32, i32, vp, i64, pi64, pvp, pvp, C.POINTER(i32), pvp], i32),
     "vkc_dense_backward": ([vp, i32, vp, vp, vp, vp, vp, vp, i64, i64, i64], i32),
     "vkc_dense_backward_act": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64], i32),
     "vkc_dense_backward_ex": ([vp, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64, i64, i64, i32], i32),

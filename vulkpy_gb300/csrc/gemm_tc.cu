@@ -642,12 +642,41 @@ __device__ __forceinline__ void add4(float4& s, const float4& a) {
   s.w += a.w;
 }
 
+// The reduction's results also written as the next GEMM's operand: K-major
+// bf16 hi (and lo) rows of pitch ldk (a multiple of 64), the split of
+// split_kmajor8_body (same values), with the padding columns [N, ldk) zero.
+__device__ __forceinline__ void split_out4(const SplitOut& so, int64_t r, int64_t col, int64_t N, float4 v) {
+  __align__(8) __nv_bfloat16 h[4], l[4];
+  split_bf16(v.x, h[0], l[0]);
+  split_bf16(v.y, h[1], l[1]);
+  split_bf16(v.z, h[2], l[2]);
+  split_bf16(v.w, h[3], l[3]);
+  *reinterpret_cast<uint2*>(so.hi + r * so.ldk + col) = *reinterpret_cast<const uint2*>(h);
+  if (so.lo) *reinterpret_cast<uint2*>(so.lo + r * so.ldk + col) = *reinterpret_cast<const uint2*>(l);
+  if (col + 4 == N)
+    for (int64_t k = N; k < so.ldk; ++k) {
+      so.hi[r * so.ldk + k] = __float2bfloat16_rn(0.f);
+      if (so.lo) so.lo[r * so.ldk + k] = __float2bfloat16_rn(0.f);
+    }
+}
+__device__ __forceinline__ void split_out1(const SplitOut& so, int64_t r, int64_t col, int64_t N, float v) {
+  __nv_bfloat16 h, l;
+  split_bf16(v, h, l);
+  so.hi[r * so.ldk + col] = h;
+  if (so.lo) so.lo[r * so.ldk + col] = l;
+  if (col + 1 == N)
+    for (int64_t k = N; k < so.ldk; ++k) {
+      so.hi[r * so.ldk + k] = __float2bfloat16_rn(0.f);
+      if (so.lo) so.lo[r * so.ldk + k] = __float2bfloat16_rn(0.f);
+    }
+}
+
 // Four columns per thread (N % 4 == 0, ldc % 4 == 0, 16-byte aligned C);
 // the split loads are issued four at a time ahead of their (ordered) adds.
 __global__ void __launch_bounds__(256)
 k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
                  float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-                 const float* __restrict__ dmask, int dact) {
+                 const float* __restrict__ dmask, int dact, SplitOut so) {
   pdl_wait();
   pdl_trigger();
   const int64_t total = M * N, quads = total / 4;
@@ -685,13 +714,14 @@ k_splitk_reduce4(const float* __restrict__ partial, int splits, int64_t M, int64
       v.w = act_deriv(v.w, y4.w, dact);
     }
     *cp = v;
+    if (so.hi) split_out4(so, r, col, N, v);
   }
 }
 
 __global__ void __launch_bounds__(256)
 k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_t N, float alpha, float beta,
                 float* __restrict__ C, int64_t ldc, const float* __restrict__ bias, int act,
-                const float* __restrict__ dmask, int dact) {
+                const float* __restrict__ dmask, int dact, SplitOut so) {
   pdl_wait();
   pdl_trigger();
   const int64_t total = M * N;
@@ -704,20 +734,22 @@ k_splitk_reduce(const float* __restrict__ partial, int splits, int64_t M, int64_
     float v = splitk_epilogue(s, alpha, beta, beta != 0.f ? *c : 0.f, bias != nullptr, bias ? bias[col] : 0.f, act);
     if (dmask) v = act_deriv(v, dmask[r * ldc + col], dact);
     *c = v;
+    if (so.hi) split_out1(so, r, col, N, v);
   }
 }
 
 int splitk_reduce(vkc_device_t dev, const float* partial, int splits, int64_t M, int64_t N, float alpha, float beta,
-                  float* C, int64_t ldc, const GemmEpilogue& epi) {
+                  float* C, int64_t ldc, const GemmEpilogue& epi, const SplitOut* out = nullptr) {
+  const SplitOut so = out ? *out : SplitOut{nullptr, nullptr, 0};
   if (N % 4 == 0 && ldc % 4 == 0 && ((uintptr_t)C & 15u) == 0 && ((uintptr_t)epi.dmask & 15u) == 0) {
     unsigned g = wave_grid(dev, k_splitk_reduce4, (size_t)(M * N / 4), 256);
     const cudaError_t e = launch_pdl(k_splitk_reduce4, dim3(g), dim3(256), 0, dev->stream, partial, splits, M, N,
-                                     alpha, beta, C, ldc, epi.bias, epi.act, epi.dmask, epi.dact);
+                                     alpha, beta, C, ldc, epi.bias, epi.act, epi.dmask, epi.dact, so);
     if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "splitk_reduce launch: %s", cudaGetErrorString(e));
   } else {
     unsigned g = stream_grid(dev, (size_t)(M * N), 256);
     const cudaError_t e = launch_pdl(k_splitk_reduce, dim3(g), dim3(256), 0, dev->stream, partial, splits, M, N,
-                                     alpha, beta, C, ldc, epi.bias, epi.act, epi.dmask, epi.dact);
+                                     alpha, beta, C, ldc, epi.bias, epi.act, epi.dmask, epi.dact, so);
     if (e != cudaSuccess) return set_error(VKC_ERR_CUDA, "splitk_reduce launch: %s", cudaGetErrorString(e));
   }
   return check_launch("splitk_reduce");
@@ -768,7 +800,7 @@ int max_clusters(Kern kern, uint32_t smem, int size) {
 template <bool X3, int BN, int STAGES, int DRAIN>
 int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, const CUtensorMap& malo,
                const CUtensorMap& mblo, int64_t M, int64_t N, int64_t K, float alpha, float beta, float* C,
-               int64_t ldc, const GemmEpilogue& epi, int splits) {
+               int64_t ldc, const GemmEpilogue& epi, int splits, const SplitOut* out) {
   using Cfg = PCfg<X3, BN, STAGES>;
   auto kern = k_gemm_tcp<X3, BN, STAGES, DRAIN>;
   static bool attr_set = false;
@@ -807,7 +839,7 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
     cudaGetLastError();
     cap = cudaStreamCaptureStatusActive;
   }
-  const int clusters = splits > 1 && cap == cudaStreamCaptureStatusNone &&
+  const int clusters = splits > 1 && cap == cudaStreamCaptureStatusNone && !out &&
                                g_cluster_splitk.load(std::memory_order_relaxed)
                            ? max_clusters(kern, Cfg::kSmem, splits)
                            : 0;
@@ -826,7 +858,9 @@ int launch_tcp(vkc_device_t dev, const CUtensorMap& ma, const CUtensorMap& mb, c
   int r = e == cudaSuccess ? check_launch("gemm_tc")
                            : set_error(VKC_ERR_CUDA, "gemm_tc launch: %s", cudaGetErrorString(e));
   if (r == VKC_OK && splits > 1 && clusters == 0)
-    r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi);
+    r = splitk_reduce(dev, partial, splits, M, N, alpha, beta, C, ldc, epi, out);
+  else if (r == VKC_OK && out)  // no reduction launch to write it: the pre-pass kernel on C
+    r = split_operands(dev, C, M, ldc, true, out->hi, out->lo, nullptr, 0, 0, true, nullptr, nullptr, N, out->ldk);
   scratch_free(dev, partial);
   return r;
 }
@@ -900,6 +934,42 @@ VKC_EXPORT int vkc_gemm_tune_clear(void) {
 
 namespace vkc {
 
+int tc_split_operands(vkc_device_t dev, const float* A, int64_t M, int64_t lda, bool a_kcontig,
+                      __nv_bfloat16* a_hi, __nv_bfloat16* a_lo, const float* B, int64_t N, int64_t ldb,
+                      bool b_kcontig, __nv_bfloat16* b_hi, __nv_bfloat16* b_lo, int64_t K, int64_t Kp) {
+  return split_operands(dev, A, M, lda, a_kcontig, a_hi, a_lo, B, N, ldb, b_kcontig, b_hi, b_lo, K, Kp);
+}
+
+// The GEMM on operands already in K-major bf16 form ([M][Kp] and [N][Kp],
+// Kp = K rounded up to 64, zero past K): tensor maps, plan, launch and
+// split-K reduction; `out` (may be NULL) also receives C in that form.
+int gemm_tc_presplit(vkc_device_t dev, int precision, int64_t M, int64_t N, int64_t K, float alpha,
+                     const __nv_bfloat16* a_hi, const __nv_bfloat16* a_lo, const __nv_bfloat16* b_hi,
+                     const __nv_bfloat16* b_lo, float beta, float* C, int64_t ldc, const GemmEpilogue& epi,
+                     const SplitOut* out) {
+  const bool x3 = precision == VKC_MM_BF16X3;
+  const int64_t Kp = (K + kBK - 1) / kBK * kBK;
+  // boxes are 64 K wide: 128 rows for a CTA's op(A) tile, bn rows for its
+  // op(B) tile
+  const TcPlan plan = choose_plan(dev, precision, M, N, K);
+  CUtensorMap ma, mb, malo, mblo;
+  int r = make_map(&ma, a_hi, M, Kp, kBM);
+  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, plan.bn);
+  if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
+  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, plan.bn);
+  if (r != VKC_OK) return r;
+  // stages fill ~192 KB of shared memory
+  if (x3 && plan.bn == 256)
+    return launch_tcp<true, 256, 2, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits,
+                                              out);
+  if (x3)
+    return launch_tcp<true, 128, 3, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits,
+                                              out);
+  if (plan.bn == 256)
+    return launch_tcp<false, 256, 4, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits, out);
+  return launch_tcp<false, 128, 6, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits, out);
+}
+
 int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_t N, int64_t K, float alpha,
             const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
             GemmEpilogue epi) {
@@ -924,25 +994,8 @@ int gemm_tc(vkc_device_t dev, int precision, bool ta, bool tb, int64_t M, int64_
   // op(A)(m,k): ta ? A[k*lda + m] : A[m*lda + k]  -> K contiguous iff !ta
   // op(B)(k,n): tb ? B[n*ldb + k] : B[k*ldb + n]  -> (n,k) K contiguous iff tb
   r = split_operands(dev, A, M, lda, !ta, a_hi, a_lo, B, N, ldb, tb, b_hi, b_lo, K, Kp);
-  // boxes are 64 K wide: 128 rows for a CTA's op(A) tile, bn rows for its
-  // op(B) tile
-  const TcPlan plan = choose_plan(dev, precision, M, N, K);
-  CUtensorMap ma, mb, malo, mblo;
-  if (r == VKC_OK) r = make_map(&ma, a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mb, b_hi, N, Kp, plan.bn);
-  if (r == VKC_OK) r = make_map(&malo, x3 ? (const void*)a_lo : (const void*)a_hi, M, Kp, kBM);
-  if (r == VKC_OK) r = make_map(&mblo, x3 ? (const void*)b_lo : (const void*)b_hi, N, Kp, plan.bn);
-  if (r == VKC_OK) {
-    // stages fill ~192 KB of shared memory
-    if (x3 && plan.bn == 256)
-      r = launch_tcp<true, 256, 2, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
-    else if (x3)
-      r = launch_tcp<true, 128, 3, kDrainX3>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
-    else if (plan.bn == 256)
-      r = launch_tcp<false, 256, 4, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
-    else
-      r = launch_tcp<false, 128, 6, 1>(dev, ma, mb, malo, mblo, M, N, K, alpha, beta, C, ldc, epi, plan.splits);
-  }
+  if (r == VKC_OK) r = gemm_tc_presplit(dev, precision, M, N, K, alpha, a_hi, a_lo, b_hi, b_lo, beta, C, ldc, epi,
+                                        nullptr);
   scratch_free(dev, scratch);
   return r;
 }

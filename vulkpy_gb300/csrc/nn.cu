@@ -472,6 +472,98 @@ VKC_EXPORT int vkc_dense_forward(vkc_device_t dev, int precision, const float* x
                   epi);
 }
 
+VKC_EXPORT int vkc_dense_stack_forward(vkc_device_t dev, int precision, int layers, const float* x, int64_t batch,
+                                       const int64_t* dims, const float* const* w, const float* const* bias,
+                                       const int* act, float* const* y) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(layers >= 1 && x && dims && w && bias && act && y, "NULL argument");
+  VKC_REQUIRE(batch >= 0, "negative size");
+  for (int l = 0; l <= layers; ++l) VKC_REQUIRE(dims[l] >= 0, "negative size");
+  for (int l = 0; l < layers; ++l) {
+    VKC_REQUIRE(act[l] >= VKC_ACT_NONE && act[l] <= VKC_ACT_SIGMOID, "unknown activation %d", act[l]);
+    VKC_REQUIRE(w[l] && y[l], "NULL buffer");
+  }
+  if (batch == 0) return VKC_OK;
+  // The chained form needs every product on the tensor-core path (the
+  // layer-by-layer calls would take it too): M > 1, N > 1, K > 0.
+  bool chain = (precision == VKC_MM_BF16 || precision == VKC_MM_BF16X3) && layers >= 2 && batch > 1 &&
+               batch < (1ll << 31) && (batch + 127) / 128 <= 65535;
+  for (int l = 0; l < layers && chain; ++l)
+    chain = dims[l] > 0 && dims[l] < (1ll << 31) && dims[l + 1] > 1 && dims[l + 1] < (1ll << 31);
+  if (!chain) {
+    const float* in = x;
+    for (int l = 0; l < layers; ++l) {
+      const int r = vkc_dense_forward(dev, precision, in, w[l], bias[l], y[l], batch, dims[l], dims[l + 1], act[l]);
+      if (r != VKC_OK) return r;
+      in = y[l];
+    }
+    return VKC_OK;
+  }
+  const bool x3 = precision == VKC_MM_BF16X3;
+  const int parts = x3 ? 2 : 1;
+  std::vector<int64_t> kp((size_t)layers);
+  size_t elems = 0;
+  for (int l = 0; l < layers; ++l) {
+    kp[(size_t)l] = (dims[l] + 63) / 64 * 64;
+    elems += (size_t)(batch + dims[l + 1]) * (size_t)kp[(size_t)l] * (size_t)parts;
+  }
+  void* scratch = nullptr;
+  int r = vkc::scratch_alloc(dev, elems * sizeof(__nv_bfloat16), &scratch);
+  if (r != VKC_OK) return r;
+  // per layer: its input [batch][Kp] and its weight [out][Kp], hi then lo
+  std::vector<__nv_bfloat16*> a_hi((size_t)layers), a_lo((size_t)layers), w_hi((size_t)layers), w_lo((size_t)layers);
+  __nv_bfloat16* p = static_cast<__nv_bfloat16*>(scratch);
+  for (int l = 0; l < layers; ++l) {
+    const size_t an = (size_t)batch * (size_t)kp[(size_t)l], wn = (size_t)dims[l + 1] * (size_t)kp[(size_t)l];
+    a_hi[(size_t)l] = p;
+    p += an;
+    a_lo[(size_t)l] = x3 ? p : nullptr;
+    p += x3 ? an : 0;
+    w_hi[(size_t)l] = p;
+    p += wn;
+    w_lo[(size_t)l] = x3 ? p : nullptr;
+    p += x3 ? wn : 0;
+  }
+  // The weights of layers 1.. are split on the side stream (they do not
+  // depend on the chain), the input and layer 0's weight on the main one.
+  const bool fork = dev->side_stream && dev->stream == dev->own_stream;
+  cudaStream_t main = dev->stream;
+  if (fork) {
+    VKC_CUDA(cudaEventRecord(dev->side_fork, main));
+    VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->side_fork, 0));
+    dev->stream = dev->side_stream;
+  }
+  for (int l = 1; l < layers && r == VKC_OK; ++l)
+    r = vkc::tc_split_operands(dev, w[l], dims[l + 1], dims[l], true, w_hi[(size_t)l], w_lo[(size_t)l], nullptr, 0, 0,
+                               true, nullptr, nullptr, dims[l], kp[(size_t)l]);
+  cudaError_t ej = cudaSuccess;
+  if (fork) {
+    dev->stream = main;
+    ej = cudaEventRecord(dev->side_join, dev->side_stream);  // recorded even after an error: a capture stays joined
+  }
+  if (r == VKC_OK)
+    r = vkc::tc_split_operands(dev, x, batch, dims[0], true, a_hi[0], a_lo[0], w[0], dims[1], dims[0], true, w_hi[0],
+                               w_lo[0], dims[0], kp[0]);
+  // each layer's reduction (or epilogue pre-pass) writes the next layer's input split
+  for (int l = 0; l < layers; ++l) {
+    if (l == 1 && fork) {
+      const cudaError_t e = ej == cudaSuccess ? cudaStreamWaitEvent(main, dev->side_join, 0) : ej;
+      if (e != cudaSuccess && r == VKC_OK) r = vkc::set_error(VKC_ERR_CUDA, "side stream join: %s", cudaGetErrorString(e));
+    }
+    if (r != VKC_OK) continue;
+    vkc::GemmEpilogue epi;
+    epi.bias = bias[l];
+    epi.act = act[l];
+    vkc::SplitOut out{l + 1 < layers ? a_hi[(size_t)l + 1] : nullptr, l + 1 < layers ? a_lo[(size_t)l + 1] : nullptr,
+                      l + 1 < layers ? kp[(size_t)l + 1] : 0};
+    r = vkc::gemm_tc_presplit(dev, precision, batch, dims[l + 1], dims[l], 1.0f, a_hi[(size_t)l], a_lo[(size_t)l],
+                              w_hi[(size_t)l], w_lo[(size_t)l], 0.0f, y[l], dims[l + 1], epi,
+                              l + 1 < layers ? &out : nullptr);
+  }
+  vkc::scratch_free(dev, scratch);
+  return r;
+}
+
 VKC_EXPORT int vkc_dense_backward(vkc_device_t dev, int precision, const float* x, const float* w, const float* dy,
                                   float* dx, float* dw, float* db, int64_t batch, int64_t in_dim, int64_t out_dim) {
   VKC_BIND(dev);

@@ -8,8 +8,9 @@ import ctypes as C
 from ..vkarray import Array
 from ..graph import Graph
 from .._lib import lib, check
+from .. import _lib
 from .core import Module, Loss
-from .layers import Dense, ReLU, Sigmoid, Softmax
+from .layers import Dense, ReLU, Sigmoid, Softmax, _PREC
 from .optimizers import AdamState, SGDState
 
 __all__ = ["Sequence", "CompiledStep"]
@@ -36,7 +37,63 @@ class Sequence:
         self.apply_regularizers = apply_regularizers
         self.fuse = fuse
 
+    def _stack_plan(self, x: Array):
+        """The (Dense, activation or None) pairs when the whole model is a
+        stack of Dense layers, each optionally followed by ReLU / Sigmoid, on
+        the tensor-core path (run by one chained call), else None."""
+        if not self.fuse or len(x.shape) != 2 or x._gpu.matmul_precision not in ("bf16", "bf16x3"):
+            return None
+        plan = []
+        i, n = 0, len(self.L)
+        while i < n:
+            layer = self.L[i]
+            if type(layer) is not Dense:
+                return None
+            nxt = self.L[i + 1] if i + 1 < n else None
+            if type(nxt) in (ReLU, Sigmoid):
+                plan.append((layer, nxt))
+                i += 2
+            else:
+                plan.append((layer, None))
+                i += 1
+        return plan if len(plan) >= 2 else None
+
+    def _forward_stack(self, x: Array, plan) -> Array:
+        """The stack in one call (vkc_dense_stack_forward: each layer's
+        split-K reduction also writes the next layer's operand pre-pass); the
+        same float32 results and the same per-layer caches as the
+        layer-by-layer path."""
+        gpu = x._gpu
+        dims = [x.shape[1]]
+        for d, _ in plan:
+            if d.input_dim != dims[-1]:
+                raise ValueError(f"Dense input width {d.input_dim} does not match {dims[-1]}")
+            dims.append(d.output_dim)
+        ys = [Array(gpu, shape=(x.shape[0], d.output_dim)) for d, _ in plan]
+        k = len(plan)
+        ptrs = lambda v: (C.c_void_p * k)(*v)
+        check(lib.vkc_dense_stack_forward(
+            x._h, _PREC[gpu.matmul_precision], k, x._dptr(), x.shape[0], (C.c_int64 * (k + 1))(*dims),
+            ptrs([d.w.value._dptr() for d, _ in plan]), ptrs([d.b.value._dptr() for d, _ in plan]),
+            (C.c_int * k)(*[a.act if a is not None else _lib.ACT_NONE for _, a in plan]),
+            ptrs([y._buf.ptr or 0 for y in ys])))
+        inp = x
+        for (d, a), y in zip(plan, ys):
+            y._written()
+            d._x = inp
+            if a is None:
+                d._y = y
+            else:
+                d._y = None
+                a._x = None
+                a._y = y
+            inp = y
+        return ys[-1]
+
     def _forward(self, x: Array) -> Array:
+        plan = self._stack_plan(x)
+        if plan is not None:
+            return self._forward_stack(x, plan)
         i = 0
         n = len(self.L)
         while i < n:
