@@ -310,11 +310,13 @@ def test_backward_chain_matches_backward_then_activation(gpu, vk, prec, B, I, Ou
 
 
 @pytest.mark.parametrize("prec", ["bf16", "bf16x3"])
-@pytest.mark.parametrize("dims,batch", [((784, 1024, 1024, 10), 256), ((100, 300, 130, 7), 37), ((64, 96, 64), 130)])
+@pytest.mark.parametrize("dims,batch", [((784, 1024, 1024, 10), 256), ((100, 300, 130, 7), 37), ((64, 96, 64), 130),
+                                        ((16, 8, 1), 5), ((16, 8, 4), 1)])
 def test_dense_stack_forward_matches_layer_by_layer(gpu, vk, prec, dims, batch):
     """vkc_dense_stack_forward (each layer's split-K reduction writing the
     next layer's operand pre-pass, weights split on a side stream) gives the
-    bits of vkc_dense_forward layer by layer, whole-K and split-K plans."""
+    bits of vkc_dense_forward layer by layer, whole-K and split-K plans;
+    shapes off the tensor-core path (N = 1, batch 1) run layer by layer."""
     import ctypes as C
     from vulkpy_gb300 import _lib, autotune
     P = {"bf16": _lib.MM_BF16, "bf16x3": _lib.MM_BF16X3}[prec]
