@@ -197,6 +197,15 @@ int vkc_set_cluster_splitk(int enable);
  * across its backward pass, so the weight GEMMs of every layer overlap the
  * chain of input-gradient GEMMs.  No reference counterpart. */
 int vkc_side_defer(vkc_device_t dev, int defer);
+/* Work on the side branch: after vkc_side_begin(dev) the device's calls go
+ * to the side stream, which first waits for everything issued so far on the
+ * device's stream and on the bias-sum branch; vkc_side_end(dev) returns to
+ * the device's stream and joins the branch back (or, under vkc_side_defer,
+ * leaves it for that join).  Sequence.train runs each layer's optimizer
+ * step there as soon as the layer's gradients are issued.  Only from the
+ * device's own stream.  No reference counterpart. */
+int vkc_side_begin(vkc_device_t dev);
+int vkc_side_end(vkc_device_t dev);
 /* Number of device and pinned-host allocations this library has requested
  * since load (vkc_alloc, vkc_upload, vkc_host_alloc and every scratch
  * allocation inside an op).  No reference counterpart; lets a caller check

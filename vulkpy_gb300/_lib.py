@@ -94,6 +94,8 @@ _SIGS = {
     "vkc_set_pdl": ([i32], i32),
     "vkc_set_cluster_splitk": ([i32], i32),
     "vkc_side_defer": ([vp, i32], i32),
+    "vkc_side_begin": ([vp], i32),
+    "vkc_side_end": ([vp], i32),
     "vkc_inject_alloc_failure": ([i64], i32),
     "vkc_binary": ([vp, i32, vp, vp, vp, sz], i32),
     "vkc_binary_scalar": ([vp, i32, vp, f32, vp, sz], i32),

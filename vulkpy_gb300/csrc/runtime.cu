@@ -603,6 +603,26 @@ VKC_EXPORT int vkc_side_defer(vkc_device_t dev, int defer) {
   return VKC_OK;
 }
 
+VKC_EXPORT int vkc_side_begin(vkc_device_t dev) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(dev->stream == dev->own_stream, "branch: not on the device's own stream");
+  VKC_CUDA(cudaEventRecord(dev->side_fork, dev->stream));
+  VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->side_fork, 0));
+  VKC_CUDA(cudaEventRecord(dev->bias_join, dev->bias_stream));
+  VKC_CUDA(cudaStreamWaitEvent(dev->side_stream, dev->bias_join, 0));
+  dev->stream = dev->side_stream;
+  dev->side_pending = 1;
+  return VKC_OK;
+}
+
+VKC_EXPORT int vkc_side_end(vkc_device_t dev) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(dev->stream == dev->side_stream, "branch: vkc_side_end without vkc_side_begin");
+  dev->stream = dev->own_stream;
+  if (!dev->side_defer) return vkc_side_defer(dev, 0);
+  return VKC_OK;
+}
+
 VKC_EXPORT int vkc_set_cluster_splitk(int enable) {
   vkc::g_cluster_splitk.store(enable ? 1 : 0, std::memory_order_relaxed);
   return VKC_OK;

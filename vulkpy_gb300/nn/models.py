@@ -114,10 +114,14 @@ class Sequence:
             i += 1
         return x
 
-    def _backward(self, accumulate: bool = True):
+    def _backward(self, accumulate: bool = True, early_update: bool = False):
         """Backward through the layers; with ``accumulate`` False the Dense
         layers overwrite their gradients (each is written once per step)
-        instead of adding to them."""
+        instead of adding to them.  ``early_update``: each Dense layer's
+        optimizer step is issued on the side branch as soon as its gradients
+        are (it waits there for them and for the layer's last use of its
+        weights, the input-gradient GEMM), so only the first layer's step
+        follows the backward on the main stream."""
         dx = self.loss.grad()
         # the Dense layers' weight GEMMs and bias sums stay on branch streams
         # until the whole backward is issued (joined back in the finally)
@@ -128,12 +132,22 @@ class Sequence:
         keep = [dx]
         check(lib.vkc_side_defer(h, 1))
         try:
-            self._backward_layers(dx, accumulate, keep)
+            self._backward_layers(dx, accumulate, keep, early_update)
         finally:
             check(lib.vkc_side_defer(h, 0))
             del keep
 
-    def _backward_layers(self, dx, accumulate: bool, keep: list):
+    def _update_early(self, dense: Dense):
+        h = dense.w.value._h
+        check(lib.vkc_side_begin(h))
+        try:
+            done = self._update_grouped([dense.w, dense.b])
+        finally:
+            check(lib.vkc_side_end(h))
+        if not done:
+            raise RuntimeError("early optimizer step without a shared Adam / SGD optimizer")
+
+    def _backward_layers(self, dx, accumulate: bool, keep: list, early_update: bool = False):
         k = len(self.L) - 1
         while k >= 0:
             layer = self.L[k]
@@ -145,6 +159,8 @@ class Sequence:
                 # same GEMM: dx is already the lower Dense layer's dy
                 dx = layer.backward_chain(dx, prev.act, prev._y, accumulate=accumulate)
                 keep.append(dx)
+                if early_update:
+                    self._update_early(layer)
                 k -= 2
                 continue
             if (self.fuse and type(layer) in (ReLU, Sigmoid) and type(prev) is Dense
@@ -153,10 +169,14 @@ class Sequence:
                 # the activation's backward and the Dense bias sum in one kernel
                 dx = prev.backward_act(dx, layer.act, layer._y, need_dx=k - 1 > 0, accumulate=accumulate)
                 keep.append(dx)
+                if early_update:
+                    self._update_early(prev)
                 k -= 2
                 continue
             if type(layer) is Dense:
                 dx = layer.backward(dx, need_dx=k > 0, accumulate=accumulate)
+                if early_update:
+                    self._update_early(layer)
             elif k == 0 and isinstance(layer, Dense):
                 layer.backward(dx, need_dx=False)
             else:
@@ -213,6 +233,19 @@ class Sequence:
         for _L in self.L:
             _L.update()
 
+    def _shares_one_optimizer(self) -> bool:
+        """Every parameter under one Adam or one SGD optimizer (the grouped
+        step's condition), on the device's own stream (branches need it)."""
+        ps = self._params()
+        if not ps:
+            return False
+        st = [p.opt_state for p in ps]
+        if any(s.opt is not st[0].opt for s in st):
+            return False
+        if not (all(type(s) is AdamState for s in st) or all(type(s) is SGDState for s in st)):
+            return False
+        return ps[0].value._gpu._dev.own_stream()
+
     def _update_grouped(self, ps) -> bool:
         """One launch for every parameter when they share one Adam or one SGD
         optimizer (per tensor the same arithmetic as Parameter.update)."""
@@ -251,11 +284,14 @@ class Sequence:
         _y = self._forward(x)
         _loss = self.loss(_y, y)
         if self.fuse and self._overwrites_grads():
-            self._backward(accumulate=False)
+            early = not self.apply_regularizers and self._shares_one_optimizer()
+            self._backward(accumulate=False, early_update=early)
+            if not early:
+                self._update()
         else:
             self._zero_grad()
             self._backward()
-        self._update()
+            self._update()
         return (_y, _loss)
 
     def predict(self, x: Array, y: Optional[Array] = None) -> Union[Array, Tuple[Array, Array]]:

@@ -139,6 +139,10 @@ class _Device:
                 lib.vkc_free(self.h, p)
 
     # -- branches -----------------------------------------------------------
+    def own_stream(self) -> bool:
+        """True when work goes to the device's own stream (no branch open)."""
+        return len(self.streams) == 1
+
     def branch_enter(self):
         parent = self.streams[-1]
         if self.spare:
