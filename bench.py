@@ -19,7 +19,7 @@ metric = algorithmic bytes of the step / step time (GB/s).  Inputs stay in
 HBM for `value`; the `e2e` leg uploads X, row, col, idx from pinned host
 memory and reads the reduction results and the final X back every step
 (pipelined: step i's read-back and step i+1's upload overlap the compute;
-30 steps per timed repetition, best of three repetitions).
+30 steps per timed repetition, best of five repetitions).
 """
 from __future__ import annotations
 
@@ -352,16 +352,36 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
         final = np.asarray(X)
         d2h = sum(o.nbytes for o in got) + final.nbytes
 
+    import ctypes
+    import gc
+    from vulkpy_gb300 import _lib
     marks = []
+    misses = []   # per iteration: (pinned host blocks, device allocations) requested
+    gcs = []      # garbage collections (generation, ms) during the timed iterations
+
+    def on_gc(phase, info):
+        if phase == "start":
+            on_gc.t = time.perf_counter()
+        else:
+            gcs.append((len(marks), info.get("generation"), round((time.perf_counter() - on_gc.t) * 1e3, 2)))
+    on_gc.t = 0.0
+
+    def counts():
+        c = ctypes.c_uint64()
+        _lib.lib.vkc_alloc_count(ctypes.byref(c))
+        return vk.vkarray._pinned_pool.allocs, c.value
 
     def run(steps):
         pending = None
         for _ in range(steps):
+            c0 = counts()
             cur = issue()
             if pending is not None:
                 collect(pending)
             pending = cur
             marks.append(time.perf_counter())
+            c1 = counts()
+            misses.append((c1[0] - c0[0], c1[1] - c0[1]))
         collect(pending)
 
     # a few more untimed steps than the kernel leg: the first pipelined steps
@@ -374,25 +394,33 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     gpu.wait()
     if dist is not None:
         dist.barrier()
-    # Three timed repetitions, the best reported (as for the CPU baseline):
-    # the host sometimes stalls for tens of milliseconds in one iteration
-    # (seen once in ~100 iterations, not reproducible in isolation).
+    # Five timed repetitions, the best reported (as for the CPU baseline):
+    # on some runs the host stalls once per repetition for 40-60 ms over two
+    # or three iterations, with no allocation, pinned-pool miss or garbage
+    # collection in them (the counts below); other runs show none.
     reps = []
-    for _ in range(3):
+    for _ in range(5):
         t0 = time.perf_counter()
         marks.clear()
+        misses.clear()
+        gcs.clear()
+        gc.callbacks.append(on_gc)
         run(args.e2e_steps)
+        gc.callbacks.remove(on_gc)
         gpu.wait()
         dt_rep = (time.perf_counter() - t0) / args.e2e_steps
         # host time of each iteration (issue step i+1, read step i), for spotting stalls
-        reps.append((dt_rep, [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)]))
-    dt_best, step_ms = min(reps, key=lambda r: r[0])
+        reps.append((dt_rep, [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)], list(misses),
+                     [g for g in gcs if g[2] >= 1.0]))
+    dt_best, step_ms, step_misses, step_gcs = min(reps, key=lambda r: r[0])
     dt = max_over_ranks(dt_best, dist)
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "iteration_ms": step_ms, "repetitions_ms": [round(r[0] * 1e3, 3) for r in reps],
+            "iteration_pinned_and_device_allocations": step_misses,
+            "gc_over_1ms": step_gcs,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
-                   "step i+1 issued before step i's results are read; best of 3 timed repetitions"}
+                   "step i+1 issued before step i's results are read; best of 5 timed repetitions"}
 
 
 # ---------------------------------------------------------------- matmul / MLP

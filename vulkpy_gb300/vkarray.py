@@ -264,6 +264,7 @@ class _PinnedPool:
         self.cached = 0
         self.limit = limit_bytes
         self.lock = threading.Lock()
+        self.allocs = 0  # blocks allocated from the driver (misses)
 
     def get(self, nbytes: int) -> Tuple[int, int]:
         cap = 1 << max(20, (nbytes - 1).bit_length())
@@ -274,6 +275,7 @@ class _PinnedPool:
                 return lst.pop(), cap
         p = C.c_void_p()
         check(lib.vkc_host_alloc(cap, C.byref(p)))
+        self.allocs += 1
         return p.value, cap
 
     def put(self, ptr: int, cap: int):
