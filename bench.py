@@ -356,7 +356,7 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     import gc
     from vulkpy_gb300 import _lib
     marks = []
-    misses = []   # per iteration: (pinned host blocks, device allocations) requested
+    misses = []   # per iteration: (pinned host blocks, device allocations requested, issue ms)
     gcs = []      # garbage collections (generation, ms) during the timed iterations
 
     def on_gc(phase, info):
@@ -375,13 +375,15 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
         pending = None
         for _ in range(steps):
             c0 = counts()
+            ta = time.perf_counter()
             cur = issue()
+            tb = time.perf_counter()
             if pending is not None:
                 collect(pending)
             pending = cur
             marks.append(time.perf_counter())
             c1 = counts()
-            misses.append((c1[0] - c0[0], c1[1] - c0[1]))
+            misses.append((c1[0] - c0[0], c1[1] - c0[1], round((tb - ta) * 1e3, 2)))
         collect(pending)
 
     # a few more untimed steps than the kernel leg: the first pipelined steps
@@ -417,7 +419,7 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "iteration_ms": step_ms, "repetitions_ms": [round(r[0] * 1e3, 3) for r in reps],
-            "iteration_pinned_and_device_allocations": step_misses,
+            "iteration_pinned_device_allocations_issue_ms": step_misses,
             "gc_over_1ms": step_gcs,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
                    "step i+1 issued before step i's results are read; best of 5 timed repetitions"}
