@@ -401,6 +401,8 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     # or three iterations, with no allocation, pinned-pool miss or garbage
     # collection in them (the counts below); other runs show none.
     reps = []
+    e2e_clocks = ClockSampler(os.environ.get("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0")).split(",")[0])
+    e2e_clocks.start()
     for _ in range(5):
         t0 = time.perf_counter()
         marks.clear()
@@ -414,13 +416,14 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
         # host time of each iteration (issue step i+1, read step i), for spotting stalls
         reps.append((dt_rep, [round((b - a) * 1e3, 2) for a, b in zip([t0] + marks[:-1], marks)], list(misses),
                      [g for g in gcs if g[2] >= 1.0]))
+    e2e_clk = e2e_clocks.stop()
     dt_best, step_ms, step_misses, step_gcs = min(reps, key=lambda r: r[0])
     dt = max_over_ranks(dt_best, dist)
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "iteration_ms": step_ms, "repetitions_ms": [round(r[0] * 1e3, 3) for r in reps],
             "iteration_pinned_device_allocations_issue_ms": step_misses,
-            "gc_over_1ms": step_gcs,
+            "gc_over_1ms": step_gcs, "clocks": e2e_clk,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
                    "step i+1 issued before step i's results are read; best of 5 timed repetitions"}
 
