@@ -414,9 +414,18 @@ int vkc_mse_grouped(vkc_device_t dev, const float* const* x, const float* const*
 
 /* ---- gather ------------------------------------------------------ */
 /* c[i] = a[idx[i]], i < n_idx.  An index >= n_a writes NaN and sets bit0 of
- * the device error word.  vkarray.py:1476-1500, gather.comp:21-26. */
+ * the device error word.  c must not overlap a.  Tables of >= 2^25 floats
+ * gathered by >= 2^21 indices (16-byte aligned idx and c) take a binned
+ * form: indices partitioned by table window in chunks of 4096, each window
+ * read while it is in L2, values put back in order -- three launches and
+ * scratch of 6 bytes per index (the direct kernel if that cannot be had).
+ * vkarray.py:1476-1500, gather.comp:21-26. */
 int vkc_gather(vkc_device_t dev, const float* a, size_t n_a, const uint32_t* idx,
                size_t n_idx, float* c);
+/* Which form vkc_gather takes: 0 = by size (default), 1 = always the direct
+ * kernel, 2 = the binned form whenever idx and c are 16-byte aligned and
+ * n_idx < 2^32.  Both give the same values.  No reference counterpart. */
+int vkc_set_gather_bins(int mode);
 /* c[k, i, j] = a[i, min(idx[k], axis-1), j]; output [n_idx, prev, post].
  * vkarray.py:1501-1521, gather_axis.comp:24-43, U32Array.to_onehot 239-253. */
 int vkc_gather_axis(vkc_device_t dev, const float* a, size_t prev, size_t axis, size_t post,
