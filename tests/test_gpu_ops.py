@@ -158,6 +158,36 @@ def test_broadcast_large_row_and_col(gpu, vk):
         np.testing.assert_array_equal(np.asarray(z), np.asarray(vk.Array(gpu, data=np.abs(X) + 0.5) ** o))
 
 
+@pytest.mark.parametrize("shape,other", [((37, 8192), (1, 8192)), ((37, 8192), (37, 1)), ((3, 5, 4096), (5, 1)),
+                                         ((2, 3, 12288), (1, 3, 12288)), ((1, 4096), (1, 1))])
+def test_inplace_broadcast_full_chunks(gpu, vk, shape, other):
+    """In place with whole 4096-column chunks (the kernel that loads a
+    block's next chunk before storing the current one): bit-exact with the
+    oracle for + - * / max min, ** equal to the out-of-place result, and an
+    in-place clamp with broadcast bounds."""
+    rng = np.random.default_rng(sum(shape))
+    X = rng.standard_normal(shape).astype(np.float32)
+    Y = rng.uniform(0.5, 2, other).astype(np.float32)
+    y = vk.Array(gpu, data=Y)
+    for op, meth in ((O.ADD, "__iadd__"), (O.SUB, "__isub__"), (O.MUL, "__imul__"), (O.DIV, "__itruediv__")):
+        z = vk.Array(gpu, data=X)
+        getattr(z, meth)(y)
+        np.testing.assert_array_equal(np.asarray(z), O.bcast(op, X, Y))
+    for op, meth in ((O.MAX, "max"), (O.MIN, "min")):
+        z = vk.Array(gpu, data=X)
+        getattr(z, meth)(y, inplace=True)
+        np.testing.assert_array_equal(np.asarray(z), O.bcast(op, X, Y))
+    z = vk.Array(gpu, data=np.abs(X) + 0.5)
+    z **= y
+    np.testing.assert_array_equal(np.asarray(z), np.asarray(vk.Array(gpu, data=np.abs(X) + 0.5) ** y))
+    lo = vk.Array(gpu, data=-Y)
+    hi = vk.Array(gpu, data=Y * 0.5)
+    z = vk.Array(gpu, data=X)
+    z.clamp(lo, hi, inplace=True)
+    np.testing.assert_array_equal(np.asarray(z), np.minimum(np.maximum(X, -Y), Y * 0.5))
+    assert gpu.check_errors() == 0
+
+
 def test_clamp_variants(gpu, vk):
     rng = np.random.default_rng(8)
     a = rng.standard_normal((33, 70)).astype(np.float32)
