@@ -356,7 +356,8 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     import gc
     from vulkpy_gb300 import _lib
     marks = []
-    misses = []   # per iteration: (pinned host blocks, device allocations requested, issue ms)
+    misses = []   # per iteration: (pinned host blocks, device allocations requested, issue ms,
+                  #                 MiB the compute / upload pools grew by)
     gcs = []      # garbage collections (generation, ms) during the timed iterations
 
     def on_gc(phase, info):
@@ -367,9 +368,10 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     on_gc.t = 0.0
 
     def counts():
-        c = ctypes.c_uint64()
+        c, rc, ru = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         _lib.lib.vkc_alloc_count(ctypes.byref(c))
-        return vk.vkarray._pinned_pool.allocs, c.value
+        _lib.lib.vkc_pool_reserved(gpu.handle, ctypes.byref(rc), ctypes.byref(ru))
+        return vk.vkarray._pinned_pool.allocs, c.value, rc.value, ru.value
 
     def run(steps):
         pending = None
@@ -383,7 +385,8 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
             pending = cur
             marks.append(time.perf_counter())
             c1 = counts()
-            misses.append((c1[0] - c0[0], c1[1] - c0[1], round((tb - ta) * 1e3, 2)))
+            misses.append((c1[0] - c0[0], c1[1] - c0[1], round((tb - ta) * 1e3, 2), (c1[2] - c0[2]) >> 20,
+                           (c1[3] - c0[3]) >> 20))
         collect(pending)
 
     # a few more untimed steps than the kernel leg: the first pipelined steps
@@ -422,7 +425,7 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     return {"value": round(world * nbytes / dt / 1e9, 1), "unit": "GB/s", "ms_per_step": round(dt * 1e3, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": args.e2e_steps,
             "iteration_ms": step_ms, "repetitions_ms": [round(r[0] * 1e3, 3) for r in reps],
-            "iteration_pinned_device_allocations_issue_ms": step_misses,
+            "iteration_pinned_device_allocations_issue_ms_pool_growth_mib": step_misses,
             "gc_over_1ms": step_gcs, "clocks": e2e_clk,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
                    "step i+1 issued before step i's results are read; best of 5 timed repetitions"}

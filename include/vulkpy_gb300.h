@@ -211,6 +211,10 @@ int vkc_side_end(vkc_device_t dev);
  * allocation inside an op).  No reference counterpart; lets a caller check
  * that a call allocated nothing. */
 int vkc_alloc_count(uint64_t* count);
+/* Device memory the device's stream-ordered pools hold now (reserved, in use
+ * or cached): the pool of the compute stream's allocations and the pool of
+ * uploads.  Diagnostics; no reference counterpart. */
+int vkc_pool_reserved(vkc_device_t dev, uint64_t* compute_bytes, uint64_t* upload_bytes);
 /* Host-side fault injection for the allocation error path (the reference
  * turns Vulkan allocation errors into RuntimeError, _vkarray.cc:32, 61-72):
  * the allocation request `after` requests from now (0 = the next one) fails

@@ -124,6 +124,7 @@ _SIGS = {
     "vkc_mse_grouped": ([vp, pvp, pvp, pvp, pi64, pi64, vp, i32], i32),
     "vkc_gather": ([vp, vp, sz, vp, sz, vp], i32),
     "vkc_set_gather_bins": ([i32], i32),
+    "vkc_pool_reserved": ([vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
     "vkc_gather_axis": ([vp, vp, sz, sz, sz, vp, sz, vp], i32),
     "vkc_arg_reduce_all": ([vp, i32, vp, sz, vp], i32),
     "vkc_arg_reduce_axis": ([vp, i32, vp, sz, sz, sz, vp], i32),

@@ -628,6 +628,19 @@ VKC_EXPORT int vkc_set_cluster_splitk(int enable) {
   return VKC_OK;
 }
 
+VKC_EXPORT int vkc_pool_reserved(vkc_device_t dev, uint64_t* compute_bytes, uint64_t* upload_bytes) {
+  VKC_BIND(dev);
+  VKC_REQUIRE(compute_bytes && upload_bytes, "NULL argument");
+  *compute_bytes = 0;
+  *upload_bytes = 0;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev->index) == cudaSuccess)
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, compute_bytes);
+  if (dev->upload_pool) cudaMemPoolGetAttribute(dev->upload_pool, cudaMemPoolAttrReservedMemCurrent, upload_bytes);
+  cudaGetLastError();
+  return VKC_OK;
+}
+
 VKC_EXPORT int vkc_alloc_count(uint64_t* count) {
   VKC_REQUIRE(count, "count is NULL");
   *count = vkc::g_allocs.load(std::memory_order_relaxed);
