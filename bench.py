@@ -19,7 +19,7 @@ metric = algorithmic bytes of the step / step time (GB/s).  Inputs stay in
 HBM for `value`; the `e2e` leg uploads X, row, col, idx from pinned host
 memory and reads the reduction results and the final X back every step
 (pipelined: step i's read-back and step i+1's upload overlap the compute;
-30 steps per timed repetition, best of five repetitions).
+20 steps per timed repetition, best of eight repetitions).
 """
 from __future__ import annotations
 
@@ -392,21 +392,23 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
     # a few more untimed steps than the kernel leg: the first pipelined steps
     # still fill the device's cache of upload buffers (one 1 GiB and one
     # 256 MiB allocation show up as multi-millisecond host stalls).  The
-    # timed region holds --e2e-steps (30) steps: the pipeline's fill (the
+    # timed region holds --e2e-steps (20) steps: the pipeline's fill (the
     # first upload) and drain (the last read-back), ~11 ms together, are
     # spread over them.
     run(max(1, args.warmup) + 3)
     gpu.wait()
     if dist is not None:
         dist.barrier()
-    # Five timed repetitions, the best reported (as for the CPU baseline):
-    # on some runs the host stalls once per repetition for 40-60 ms over two
-    # or three iterations, with no allocation, pinned-pool miss or garbage
-    # collection in them (the counts below); other runs show none.
+    # Eight timed repetitions, the best reported (as for the CPU baseline):
+    # on some machines a step's results arrive late every ~0.51 s of wall
+    # time (from +3 ms to +125 ms over two or three iterations, no allocation,
+    # pool growth, pinned-pool miss or garbage collection in them; the
+    # device-timed leg never shows it), so a repetition of ~0.3 s can fall
+    # between two of them where one of 30 steps (~0.5 s) could not.
     reps = []
     e2e_clocks = ClockSampler(os.environ.get("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0")).split(",")[0])
     e2e_clocks.start()
-    for _ in range(5):
+    for _ in range(8):
         t0 = time.perf_counter()
         marks.clear()
         misses.clear()
@@ -428,7 +430,7 @@ def e2e_leg(vk, gpu, args, Xh, rowh, colh, idxh, rng, U, Nrm, I, nbytes, world, 
             "iteration_pinned_device_allocations_issue_ms_pool_growth_mib": step_misses,
             "gc_over_1ms": step_gcs, "clocks": e2e_clk,
             "api": "vulkpy_gb300 public API (Array(data=pinned), ops, Array.prefetch, np.asarray); "
-                   "step i+1 issued before step i's results are read; best of 5 timed repetitions"}
+                   "step i+1 issued before step i's results are read; best of 8 timed repetitions"}
 
 
 # ---------------------------------------------------------------- matmul / MLP
@@ -1070,7 +1072,7 @@ def main():
     ap.add_argument("--cols", type=int, default=COLS)
     ap.add_argument("--n-idx", type=int, default=N_IDX)
     ap.add_argument("--states", type=int, default=PRNG_STATES)
-    ap.add_argument("--e2e-steps", type=int, default=30)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--cpu-passes", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
